@@ -1,0 +1,79 @@
+/*
+ * kfft_gb300.h -- additive entry points of the GB300 FFT engine.
+ *
+ * The reference LibKFFT has no batch API: its callers loop over sequences on
+ * the host (ext/2d/kfft_cpx2.c:100-104 is the pattern).  These entry points
+ * are new symbols only; no reference signature changes.  They let a caller
+ * hand many sequences to the GPU in one call, pass device pointers and a CUDA
+ * stream, and run a whole batch of uneven lengths as one graph launch.
+ */
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/*
+ * Batched complex transform: `batch` sequences of plan->nfft points stored back
+ * to back.  fin/fout may be host or device memory (fin == fout allowed).
+ * Synchronous, like kfft_eval_cpx.  Same return codes as kfft_eval_cpx.
+ */
+KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* fin,
+                                           kfft_cpx* fout, uint32_t batch);
+
+/*
+ * Asynchronous batched complex transform on `stream` (a cudaStream_t, NULL =
+ * the legacy default stream).  fin/fout must be device memory.  Returns after
+ * the kernels are queued.  Calls sharing a plan must be ordered on one stream.
+ */
+KFFT_API kfft_return_t kfft_eval_cpx_async(kfft_plan_cpx* plan, const kfft_cpx* fin,
+                                           kfft_cpx* fout, uint32_t batch, void* stream);
+
+/* Batched real transforms; the spectrum of sequence b starts at b * nbins,
+ * nbins = N/2+1 for even N without KFFT_FLAG_EXPAND_SCALAR, else N. */
+KFFT_API kfft_return_t kfft_eval_scalar_batch(kfft_plan_sclr* plan, const kfft_scalar* fin,
+                                              kfft_cpx* fout, uint32_t batch);
+KFFT_API kfft_return_t kfft_evali_scalar_batch(kfft_plan_sclr* plan, const kfft_cpx* fin,
+                                               kfft_scalar* fout, uint32_t batch);
+
+/*
+ * Uneven-length batch: `count` complex sequences with lengths[i] points each,
+ * packed back to back (sequence i starts at the sum of the previous lengths).
+ * The plan groups equal lengths, builds one device plan per distinct length
+ * and records the whole batch into a CUDA graph that kfft_eval_cpx_uneven
+ * launches once per call.
+ */
+typedef struct kfft_plan_uneven kfft_plan_uneven;
+
+KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t* lengths,
+                                                  uint32_t flags);
+/* Host or device buffers of kfft_uneven_total(plan) points each; synchronous. */
+KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_cpx* fin,
+                                            kfft_cpx* fout);
+/* Device buffers only; queued on `stream` (cudaStream_t). */
+KFFT_API kfft_return_t kfft_eval_cpx_uneven_async(kfft_plan_uneven* plan, const kfft_cpx* fin,
+                                                  kfft_cpx* fout, void* stream);
+KFFT_API uint64_t kfft_uneven_total(const kfft_plan_uneven* plan);
+KFFT_API void kfft_release_uneven(kfft_plan_uneven* plan);
+
+/* Engine introspection (used by tests and the benchmark). */
+typedef struct {
+    uint64_t kernel_launches; /* kernels this library launched since load */
+    uint64_t graph_launches;  /* CUDA graphs it launched */
+    uint64_t device_bytes;    /* bytes of device memory it currently holds */
+    int32_t device;           /* CUDA device ordinal in use, -1 if none */
+    int32_t last_cuda_error;  /* last CUDA error seen (cudaError_t), 0 if none */
+} kfft_gb300_stats_t;
+
+KFFT_API void kfft_gb300_stats(kfft_gb300_stats_t* stats);
+/* Human-readable description of the last CUDA error, "" if none. */
+KFFT_API const char* kfft_gb300_last_error(void);
+/* Passes of a plan as text ("R=64 Ns=1 radices=16,4 | ..."), for diagnostics. */
+KFFT_API const char* kfft_gb300_describe(const kfft_plan_cpx* plan);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,1182 @@
+// api.cu -- the C ABI of the GB300 FFT engine (drop-in for the reference kfft.h).
+//
+// Every exported function keeps the reference's name, argument meaning and
+// error behaviour; the comment above each cites the reference definition it
+// replaces.  Plans keep kfft_object_t as their first member (KFFT_PLAN_MMGR)
+// and live in a kfft_pool_t exactly as the reference's do
+// (KFFT_ALGO_PLAN_PREPARE, incs/kfft_algo.h:15-39): NULL pool and NULL lenmem
+// creates a private pool, a non-NULL lenmem with NULL pool is a size query,
+// a user pool receives the plan (KFFT_FLAG_RENEW clears it first).  The device
+// side of each plan (its HBM arena of FP64-generated tables) is registered in
+// the pool and freed with it.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "kfft.h"
+
+using namespace kfft;
+
+// ===========================================================================
+// runtime state
+// ===========================================================================
+namespace kfft {
+static std::atomic<uint64_t> g_launches{0};
+static std::atomic<uint64_t> g_graphs{0};
+static std::atomic<int64_t> g_bytes{0};
+static std::atomic<int> g_last_err{0};
+static std::mutex g_err_mu;
+static std::string g_err_text;
+static int g_device = -1;
+static std::once_flag g_dev_once;
+
+void count_launch(int64_t n) { g_launches += uint64_t(n); }
+void count_graph_launch() { g_graphs += 1; }
+void account_device_bytes(int64_t d) { g_bytes += d; }
+
+void note_cuda_error(cudaError_t e) {
+    if (e == cudaSuccess) return;
+    g_last_err = int(e);
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err_text = cudaGetErrorString(e);
+}
+
+bool ensure_device() {
+    std::call_once(g_dev_once, [] {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            g_device = -1;
+            std::lock_guard<std::mutex> lk(g_err_mu);
+            g_err_text = "no CUDA device available";
+            return;
+        }
+        int d = 0;
+        cudaGetDevice(&d);
+        g_device = d;
+    });
+    if (g_device < 0) return false;
+    cudaSetDevice(g_device);
+    return true;
+}
+
+int current_device() { return g_device; }
+}  // namespace kfft
+
+// ===========================================================================
+// device plan handle, placed in the plan's pool
+// ===========================================================================
+struct kfft_gpu_plan {
+    DeviceArena* arena = nullptr;
+    FftPlan* plan = nullptr;      // complex transform (or the basis of a real plan)
+    const vec2_t* super_tw = nullptr;  // real transform post/pre twiddles
+    std::mutex* mu = nullptr;
+    void* ws = nullptr;  // cached device workspace
+    size_t ws_size = 0;
+    void release() {
+        if (ws) {
+            cudaFree(ws);
+            account_device_bytes(-int64_t(ws_size));
+        }
+        ws = nullptr;
+        ws_size = 0;
+        delete plan;
+        plan = nullptr;
+        delete arena;
+        arena = nullptr;
+        delete mu;
+        mu = nullptr;
+    }
+    // returns a device workspace of at least `bytes`, growing the cached one
+    void* workspace(size_t bytes) {
+        if (bytes <= ws_size) return ws;
+        if (ws) {
+            cudaFree(ws);
+            account_device_bytes(-int64_t(ws_size));
+            ws = nullptr;
+            ws_size = 0;
+        }
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            note_cuda_error(e);
+            return nullptr;
+        }
+        ws = p;
+        ws_size = bytes;
+        account_device_bytes(int64_t(bytes));
+        return ws;
+    }
+};
+
+namespace {
+struct PoolRegistry {
+    std::vector<kfft_gpu_plan*> plans;
+};
+
+size_t gpu_handle_bytes() { return (sizeof(kfft_gpu_plan) + 15) & ~size_t(15); }
+
+void registry_release(kfft_pool_t* A) {
+    if (!A || !A->device) return;
+    PoolRegistry* r = static_cast<PoolRegistry*>(A->device);
+    for (kfft_gpu_plan* g : r->plans) g->release();
+    r->plans.clear();
+}
+
+kfft_gpu_plan* new_gpu_handle(kfft_pool_t* A) {
+    void* mem = kfft_pool_alloc(A, gpu_handle_bytes());
+    if (!mem) return nullptr;
+    kfft_gpu_plan* g = new (mem) kfft_gpu_plan();
+    g->mu = new std::mutex();
+    g->arena = new DeviceArena();
+    if (!A->device) A->device = new PoolRegistry();
+    static_cast<PoolRegistry*>(A->device)->plans.push_back(g);
+    return g;
+}
+
+bool is_device_pointer(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Shared stream of synchronous evaluations on this host thread.
+cudaStream_t sync_stream() { return cudaStreamPerThread; }
+
+kfft_return_t finish(cudaStream_t st) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        return KFFT_RET_BUFFER_FAIL;
+    }
+    return KFFT_RET_SUCCESS;
+}
+
+real_t inverse_scale(uint32_t flags, uint32_t n) {
+    if (!(flags & KFFT_FLAG_INVERSE) || (flags & KFFT_FLAG_DISABLE_NORM) || n == 0) return real_t(1);
+    return real_t(1.0 / double(n));
+}
+
+// Staged view of a caller buffer on the device.
+struct Staged {
+    void* dev = nullptr;
+    bool host = false;
+};
+
+// Workspace carved out of one device allocation: [staging | engine workspace].
+struct Carve {
+    char* base = nullptr;
+    size_t used = 0, size = 0;
+    void* take(size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        if (used + bytes > size) return nullptr;
+        void* p = base + used;
+        used += bytes;
+        return p;
+    }
+};
+
+size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Runs the complex transform of `g` on device buffers.
+bool run_cpx(const FftPlan& P, const vec2_t* din, vec2_t* dout, uint32_t batch, real_t scale,
+             void* wsmem, size_t wsbytes, cudaStream_t st) {
+    Workspace ws;
+    ws.base = static_cast<char*>(wsmem);
+    ws.size = wsbytes;
+    Layout l;
+    l.batch = batch;
+    l.bs = P.N;
+    std::vector<PassDesc> descs;
+    if (!build_passes(P, din, l, dout, l, scale, ws, descs)) return false;
+    run_passes(descs, st);
+    return true;
+}
+
+// Column transform of a (rows=y, cols=x) complex array in place.
+bool run_columns(const FftPlan& Py, vec2_t* data, uint32_t x, uint32_t y, real_t scale,
+                 Carve& cv, cudaStream_t st) {
+    if (Py.method == METHOD_DIRECT) {
+        Layout l;
+        l.batch = x;
+        l.bs = 1;
+        l.es = x;
+        l.order = ORDER_B;
+        size_t wb = workspace_bytes(Py, x);
+        Workspace ws;
+        ws.base = static_cast<char*>(cv.take(wb));
+        ws.size = wb;
+        if (wb && !ws.base) return false;
+        std::vector<PassDesc> descs;
+        if (!build_passes(Py, data, l, data, l, scale, ws, descs)) return false;
+        run_passes(descs, st);
+        return true;
+    }
+    const size_t n = size_t(x) * y;
+    vec2_t* t1 = static_cast<vec2_t*>(cv.take(n * sizeof(vec2_t)));
+    vec2_t* t2 = static_cast<vec2_t*>(cv.take(n * sizeof(vec2_t)));
+    size_t wb = workspace_bytes(Py, x);
+    void* w = cv.take(wb);
+    if (!t1 || !t2 || (wb && !w)) return false;
+    launch_transpose(data, t1, y, x, 1, st);
+    if (!run_cpx(Py, t1, t2, x, scale, w, wb, st)) return false;
+    launch_transpose(t2, data, x, y, 1, st);
+    return true;
+}
+
+size_t columns_bytes(const FftPlan& Py, uint32_t x, uint32_t y) {
+    if (Py.method == METHOD_DIRECT) return r256(workspace_bytes(Py, x));
+    return 2 * r256(sizeof(vec2_t) * size_t(x) * y) + r256(workspace_bytes(Py, x));
+}
+
+struct EvalGuard {
+    std::unique_lock<std::mutex> lk;
+    explicit EvalGuard(kfft_gpu_plan* g) : lk(*g->mu) {}
+};
+
+}  // namespace
+
+// ===========================================================================
+// pool (kfft_pool.c:33-96)
+// ===========================================================================
+extern "C" {
+
+KFFT_API kfft_pool_t* kfft_pool_create(const size_t size) {
+    const size_t memneed = sizeof(kfft_pool_t) + size;
+    kfft_pool_t* p = static_cast<kfft_pool_t*>(malloc(memneed));
+    if (!p) return NULL;
+    memset(p, 0, sizeof(kfft_pool_t));
+    p->allocated = memneed;
+    p->align = 0;
+    p->head = p->area;
+    p->tail = p->area + size;
+    p->cur = p->head;
+    p->device = NULL;
+    return p;
+}
+
+KFFT_API void* kfft_pool_alloc(kfft_pool_t* A, const size_t nmem) {
+    static std::mutex mu;  // pool allocation is serialised (kfft_pool.c:57)
+    if (!A || nmem == 0) return NULL;
+    std::lock_guard<std::mutex> lk(mu);
+    if (A->cur + nmem > A->tail) return NULL;
+    uint8_t* r = A->cur;
+    A->cur += nmem;
+    return r;
+}
+
+KFFT_API size_t kfft_pool_empty(const kfft_pool_t* A) {
+    return A ? size_t(A->tail - A->cur) : 0;
+}
+
+KFFT_API void kfft_pool_zmem(const kfft_pool_t* A, void* ptr, const size_t size) {
+    if (A && ptr && size > 0 && static_cast<uint8_t*>(ptr) + size <= A->tail) memset(ptr, 0, size);
+}
+
+KFFT_API void kfft_pool_clear(kfft_pool_t* A) {
+    if (!A) return;
+    registry_release(A);
+    kfft_pool_zmem(A, A->area, size_t(A->tail - A->head));
+    A->cur = A->head;
+}
+
+KFFT_API void kfft_pool_free(kfft_pool_t* A) {
+    if (!A) return;
+    registry_release(A);
+    delete static_cast<PoolRegistry*>(A->device);
+    A->device = NULL;
+    free(A);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// plan construction protocol (incs/kfft_algo.h:15-51)
+// ===========================================================================
+namespace {
+
+template <typename T>
+T* plan_prepare(uint32_t flags, size_t memneed, kfft_pool_t* A, size_t* lenmem,
+                kfft_pool_t** owner) {
+    T* plan = nullptr;
+    kfft_pool_t* mm = nullptr;
+    if (lenmem == NULL) {
+        mm = A ? A : kfft_pool_create(memneed);
+        if (mm) {
+            if (A && (flags & KFFT_FLAG_RENEW)) kfft_pool_clear(mm);
+            plan = static_cast<T*>(kfft_pool_alloc(mm, sizeof(T)));
+        }
+        if (!plan && !A) kfft_pool_free(mm);
+    } else {
+        if (A && *lenmem >= memneed) {
+            mm = A;
+            if (flags & KFFT_FLAG_RENEW) kfft_pool_clear(mm);
+            plan = static_cast<T*>(kfft_pool_alloc(mm, sizeof(T)));
+        }
+        if (!plan) *lenmem = memneed;
+    }
+    if (plan) {
+        memset(plan, 0, sizeof(T));
+        plan->object.mmgr = mm;
+    }
+    *owner = mm;
+    return plan;
+}
+
+template <typename T>
+void plan_terminate(T* plan, kfft_pool_t* A) {
+    if (A == NULL && plan) kfft_pool_free(plan->object.mmgr);
+}
+
+// host bytes of a complex plan in a pool
+size_t cpx_memneed(uint32_t nfft) {
+    return sizeof(kfft_plan_cpx) + (nfft ? gpu_handle_bytes() + 16 : 0);
+}
+
+// builds the device side of a complex plan node allocated in pool mm
+bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm) {
+    P->nfft = nfft;
+    P->flags = flags;
+    P->level = 0;
+    if (nfft == 0) return true;
+    if (!ensure_device()) return false;
+    kfft_gpu_plan* g = new_gpu_handle(mm);
+    if (!g) return false;
+    const int sign = (flags & KFFT_FLAG_INVERSE) ? +1 : -1;
+    cudaStream_t st = sync_stream();
+    g->plan = make_plan(nfft, sign, *g->arena, st);
+    if (!g->plan) return false;
+    if (finish(st) != KFFT_RET_SUCCESS) return false;
+    P->gpu = g;
+    const FftPlan& fp = *g->plan;
+    P->method = fp.method;
+    P->prm_count = fp.method == METHOD_DIRECT ? 0 : 1;
+    const FftPlan& dp = fp.method == METHOD_DIRECT ? fp : *fp.sub_fwd;
+    uint32_t rem = dp.N;
+    P->fac_count = 0;
+    for (size_t i = 0; i < dp.passes.size() && i < MAX_FACTORS; ++i) {
+        rem /= dp.passes[i].R;
+        P->factors[2 * i] = dp.passes[i].R;
+        P->factors[2 * i + 1] = rem;
+        P->fac_count++;
+    }
+    return true;
+}
+
+}  // namespace
+
+// ===========================================================================
+// complex 1D (kfft_cpx.c:315-366)
+// ===========================================================================
+extern "C" {
+
+KFFT_API kfft_plan_cpx* kfft_config_cpx(const uint32_t nfft, const uint32_t flags, kfft_pool_t* A,
+                                        size_t* lenmem) {
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_cpx* P = plan_prepare<kfft_plan_cpx>(flags, cpx_memneed(nfft), A, lenmem, &mm);
+    if (!P) return NULL;
+    if (!cpx_init(P, nfft, flags, mm)) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* fin,
+                                           kfft_cpx* fout, uint32_t batch) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->gpu;
+    if (!g || !g->plan) return KFFT_RET_IMPROPER_PLAN;
+    EvalGuard guard(g);
+    cudaSetDevice(current_device());
+    cudaStream_t st = sync_stream();
+    const FftPlan& P = *g->plan;
+    const size_t bytes = sizeof(vec2_t) * size_t(P.N) * batch;
+    const bool hin = !is_device_pointer(fin), hout = !is_device_pointer(fout);
+    const size_t wsb = workspace_bytes(P, batch);
+    size_t need = r256(wsb) + (hin ? r256(bytes) : 0) + (hout ? r256(bytes) : 0);
+    Carve cv;
+    cv.base = static_cast<char*>(g->workspace(need));
+    cv.size = need;
+    if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;
+    const vec2_t* din = reinterpret_cast<const vec2_t*>(fin);
+    vec2_t* dout = reinterpret_cast<vec2_t*>(fout);
+    vec2_t* stage_in = nullptr;
+    if (hin) {
+        stage_in = static_cast<vec2_t*>(cv.take(bytes));
+        cudaMemcpyAsync(stage_in, fin, bytes, cudaMemcpyHostToDevice, st);
+        din = stage_in;
+    }
+    if (hout) dout = (hin && fin == fout) ? stage_in : static_cast<vec2_t*>(cv.take(bytes));
+    void* w = cv.take(wsb);
+    if (!run_cpx(P, din, dout, batch, inverse_scale(plan->flags, plan->nfft), w, wsb, st))
+        return KFFT_RET_BUFFER_FAIL;
+    if (hout) cudaMemcpyAsync(fout, dout, bytes, cudaMemcpyDeviceToHost, st);
+    return finish(st);
+}
+
+KFFT_API kfft_return_t kfft_eval_cpx(kfft_plan_cpx* plan, const kfft_cpx* fin, kfft_cpx* fout) {
+    return kfft_eval_cpx_batch(plan, fin, fout, 1);
+}
+
+KFFT_API kfft_return_t kfft_eval_cpx_async(kfft_plan_cpx* plan, const kfft_cpx* fin,
+                                           kfft_cpx* fout, uint32_t batch, void* stream) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->gpu;
+    if (!g || !g->plan) return KFFT_RET_IMPROPER_PLAN;
+    EvalGuard guard(g);
+    cudaSetDevice(current_device());
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const FftPlan& P = *g->plan;
+    const size_t wsb = workspace_bytes(P, batch);
+    void* w = wsb ? g->workspace(wsb) : nullptr;
+    if (wsb && !w) return KFFT_RET_BUFFER_FAIL;
+    if (!run_cpx(P, reinterpret_cast<const vec2_t*>(fin), reinterpret_cast<vec2_t*>(fout), batch,
+                 inverse_scale(plan->flags, plan->nfft), w, wsb, st))
+        return KFFT_RET_BUFFER_FAIL;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        return KFFT_RET_BUFFER_FAIL;
+    }
+    return KFFT_RET_SUCCESS;
+}
+
+// ===========================================================================
+// real ("scalar") 1D (kfft_scalar.c:295-329)
+// ===========================================================================
+KFFT_API kfft_plan_sclr* kfft_config_scalar(const uint32_t nfft, const uint32_t flags,
+                                            kfft_pool_t* A, size_t* lenmem) {
+    const uint32_t basis_n = (nfft % 2) ? nfft : nfft / 2;
+    const size_t memneed = sizeof(kfft_plan_sclr) + cpx_memneed(basis_n) + gpu_handle_bytes() + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_sclr* P = plan_prepare<kfft_plan_sclr>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = nfft;
+    P->flags = flags;
+    P->basis = static_cast<kfft_plan_cpx*>(kfft_pool_alloc(mm, sizeof(kfft_plan_cpx)));
+    if (!P->basis) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    memset(P->basis, 0, sizeof(kfft_plan_cpx));
+    P->basis->object.mmgr = mm;
+    if (!cpx_init(P->basis, basis_n, KFFT_CHECK_FLAGS(flags), mm)) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    if (nfft % 2 == 0 && nfft > 0) {
+        kfft_gpu_plan* g = new_gpu_handle(mm);
+        if (!g) {
+            plan_terminate(P, A);
+            return NULL;
+        }
+        const uint32_t h = nfft / 2;
+        vec2_t* t = static_cast<vec2_t*>(g->arena->alloc(sizeof(vec2_t) * (h ? h : 1)));
+        if (!t) {
+            plan_terminate(P, A);
+            return NULL;
+        }
+        gen_super_twiddles(t, h, (flags & KFFT_FLAG_INVERSE) ? +1 : -1, sync_stream());
+        if (finish(sync_stream()) != KFFT_RET_SUCCESS) {
+            plan_terminate(P, A);
+            return NULL;
+        }
+        g->super_tw = t;
+        P->gpu = g;
+    }
+    return P;
+}
+
+namespace {
+uint32_t real_bins(const kfft_plan_sclr* p) {
+    const uint32_t n = p->nfft;
+    if (n % 2 || (p->flags & KFFT_FLAG_EXPAND_SCALAR)) return n;
+    return n / 2 + 1;
+}
+
+// forward real transform on device buffers; spectrum stride `bins`
+bool real_forward_dev(const kfft_plan_sclr* p, const real_t* din, vec2_t* dout, uint32_t batch,
+                      uint64_t out_bs, int expand, Carve& cv, cudaStream_t st) {
+    const uint32_t n = p->nfft;
+    const FftPlan& B = *p->basis->gpu->plan;
+    if (n % 2) {
+        vec2_t* w = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * size_t(n) * batch));
+        size_t wb = workspace_bytes(B, batch);
+        void* ws = cv.take(wb);
+        if (!w || (wb && !ws)) return false;
+        launch_widen(din, w, uint64_t(n) * batch, st);
+        Workspace wsp;
+        wsp.base = static_cast<char*>(ws);
+        wsp.size = wb;
+        Layout li;
+        li.batch = batch;
+        li.bs = n;
+        Layout lo = li;
+        lo.bs = out_bs;
+        std::vector<PassDesc> d;
+        if (!build_passes(B, w, li, dout, lo, real_t(1), wsp, d)) return false;
+        run_passes(d, st);
+        return true;
+    }
+    const uint32_t h = n / 2;
+    vec2_t* z = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * size_t(h) * batch));
+    size_t wb = workspace_bytes(B, batch);
+    void* ws = cv.take(wb);
+    if (!z || (wb && !ws)) return false;
+    if (!run_cpx(B, reinterpret_cast<const vec2_t*>(din), z, batch, real_t(1), ws, wb, st))
+        return false;
+    launch_real_post(z, dout, p->gpu->super_tw, h, batch, out_bs, expand, st);
+    return true;
+}
+
+size_t real_forward_bytes(const kfft_plan_sclr* p, uint32_t batch) {
+    const uint32_t n = p->nfft;
+    const FftPlan& B = *p->basis->gpu->plan;
+    const uint32_t m = (n % 2) ? n : n / 2;
+    return r256(sizeof(vec2_t) * size_t(m) * batch) + r256(workspace_bytes(B, batch));
+}
+
+// inverse real transform on device buffers; spectrum stride in_bs
+bool real_inverse_dev(const kfft_plan_sclr* p, const vec2_t* din, uint64_t in_bs, real_t* dout,
+                      uint32_t batch, Carve& cv, cudaStream_t st) {
+    const uint32_t n = p->nfft;
+    const FftPlan& B = *p->basis->gpu->plan;
+    if (n % 2) {
+        vec2_t* w = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * size_t(n) * batch));
+        size_t wb = workspace_bytes(B, batch);
+        void* ws = cv.take(wb);
+        if (!w || (wb && !ws)) return false;
+        Workspace wsp;
+        wsp.base = static_cast<char*>(ws);
+        wsp.size = wb;
+        Layout li;
+        li.batch = batch;
+        li.bs = in_bs;
+        Layout lo = li;
+        lo.bs = n;
+        std::vector<PassDesc> d;
+        if (!build_passes(B, din, li, w, lo, inverse_scale(p->flags, n), wsp, d)) return false;
+        run_passes(d, st);
+        launch_narrow(w, dout, uint64_t(n) * batch, st);
+        return true;
+    }
+    const uint32_t h = n / 2;
+    vec2_t* z = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * size_t(h) * batch));
+    size_t wb = workspace_bytes(B, batch);
+    void* ws = cv.take(wb);
+    if (!z || (wb && !ws)) return false;
+    launch_real_pre(din, z, p->gpu->super_tw, h, batch, in_bs, st);
+    // the N/2-point basis normalises by 2/N: the reference's even-N inverse returns 2*x
+    return run_cpx(B, z, reinterpret_cast<vec2_t*>(dout), batch, inverse_scale(p->flags, h), ws, wb,
+                   st);
+}
+
+size_t real_inverse_bytes(const kfft_plan_sclr* p, uint32_t batch) {
+    return real_forward_bytes(p, batch);
+}
+}  // namespace
+
+KFFT_API kfft_return_t kfft_eval_scalar_batch(kfft_plan_sclr* plan, const kfft_scalar* fin,
+                                              kfft_cpx* fout, uint32_t batch) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (!plan->basis || (plan->basis->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
+    if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->basis->gpu;
+    EvalGuard guard(g);
+    cudaSetDevice(current_device());
+    cudaStream_t st = sync_stream();
+    const uint32_t bins = real_bins(plan);
+    const size_t ib = sizeof(real_t) * size_t(plan->nfft) * batch;
+    const size_t ob = sizeof(vec2_t) * size_t(bins) * batch;
+    const bool hin = !is_device_pointer(fin), hout = !is_device_pointer(fout);
+    size_t need = real_forward_bytes(plan, batch) + (hin ? r256(ib) : 0) + (hout ? r256(ob) : 0);
+    Carve cv;
+    cv.base = static_cast<char*>(g->workspace(need));
+    cv.size = need;
+    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    const real_t* din = reinterpret_cast<const real_t*>(fin);
+    vec2_t* dout = reinterpret_cast<vec2_t*>(fout);
+    if (hin) {
+        void* s = cv.take(ib);
+        cudaMemcpyAsync(s, fin, ib, cudaMemcpyHostToDevice, st);
+        din = static_cast<const real_t*>(s);
+    }
+    if (hout) dout = static_cast<vec2_t*>(cv.take(ob));
+    if (!real_forward_dev(plan, din, dout, batch, bins,
+                          (plan->flags & KFFT_FLAG_EXPAND_SCALAR) ? 1 : 0, cv, st))
+        return KFFT_RET_BUFFER_FAIL;
+    if (hout) cudaMemcpyAsync(fout, dout, ob, cudaMemcpyDeviceToHost, st);
+    return finish(st);
+}
+
+KFFT_API kfft_return_t kfft_eval_scalar(kfft_plan_sclr* plan, const kfft_scalar* fin,
+                                        kfft_cpx* fout) {
+    return kfft_eval_scalar_batch(plan, fin, fout, 1);
+}
+
+KFFT_API kfft_return_t kfft_evali_scalar_batch(kfft_plan_sclr* plan, const kfft_cpx* fin,
+                                               kfft_scalar* fout, uint32_t batch) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (!plan->basis || !(plan->basis->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
+    if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->basis->gpu;
+    EvalGuard guard(g);
+    cudaSetDevice(current_device());
+    cudaStream_t st = sync_stream();
+    const uint32_t bins = real_bins(plan);
+    const size_t ib = sizeof(vec2_t) * size_t(bins) * batch;
+    const size_t ob = sizeof(real_t) * size_t(plan->nfft) * batch;
+    const bool hin = !is_device_pointer(fin), hout = !is_device_pointer(fout);
+    size_t need = real_inverse_bytes(plan, batch) + (hin ? r256(ib) : 0) + (hout ? r256(ob) : 0);
+    Carve cv;
+    cv.base = static_cast<char*>(g->workspace(need));
+    cv.size = need;
+    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    const vec2_t* din = reinterpret_cast<const vec2_t*>(fin);
+    real_t* dout = reinterpret_cast<real_t*>(fout);
+    if (hin) {
+        void* s = cv.take(ib);
+        cudaMemcpyAsync(s, fin, ib, cudaMemcpyHostToDevice, st);
+        din = static_cast<const vec2_t*>(s);
+    }
+    if (hout) dout = static_cast<real_t*>(cv.take(ob));
+    if (!real_inverse_dev(plan, din, bins, dout, batch, cv, st)) return KFFT_RET_BUFFER_FAIL;
+    if (hout) cudaMemcpyAsync(fout, dout, ob, cudaMemcpyDeviceToHost, st);
+    return finish(st);
+}
+
+KFFT_API kfft_return_t kfft_evali_scalar(kfft_plan_sclr* plan, const kfft_cpx* fin,
+                                         kfft_scalar* fout) {
+    return kfft_evali_scalar_batch(plan, fin, fout, 1);
+}
+
+// ===========================================================================
+// service API (kfft_ext.c:6-95)
+// ===========================================================================
+KFFT_API void kfft_info(kfft_info_t* info) {
+    if (!info) return;
+    info->vmajor = KFFT_MAJOR_VERSION;
+    info->vminor = KFFT_MINOR_VERSION;
+    info->vpatch = KFFT_PATCH_VERSION;
+    info->flags = KFFT_INFO_USE_SYSMATH | KFFT_INFO_RADER_ALGO;
+#if defined(KFFT_HALF_SCALAR)
+    info->flags |= KFFT_INFO_HALF_SCALAR;
+#endif
+}
+
+KFFT_API uint32_t kfft_next_fast_size(uint32_t n) {
+    while (1) {
+        uint32_t m = n;
+        while ((m % 2) == 0) m /= 2;
+        while ((m % 3) == 0) m /= 3;
+        while ((m % 5) == 0) m /= 5;
+        if (m <= 1) break;
+        n++;
+    }
+    return n;
+}
+
+KFFT_API void* kfft_malloc(uint32_t sz) {
+    void* p = nullptr;
+    if (posix_memalign(&p, 64, sz ? sz : 1) != 0) return NULL;
+    return p;
+}
+
+KFFT_API void kfft_free_null(void** mem) {
+    if (!mem) return;
+    free(*mem);
+    *mem = NULL;
+}
+
+KFFT_API kfft_return_t kfft_cleanup(void* mem) {
+    if (!mem) return KFFT_RET_FREE_NULL;
+    kfft_object_t* M = static_cast<kfft_object_t*>(mem);
+    if (M->mmgr == NULL) return KFFT_RET_FREE_NULL;
+    kfft_pool_free(M->mmgr);
+    return KFFT_RET_SUCCESS;
+}
+
+static const char* kErrors[] = {"Success operation result",
+                                "Internal allocation memory fail",
+                                "Temporary buffer allocation fail",
+                                "Invalide free() operation for NULL buffer",
+                                "Use improper real function for this plan",
+                                "Use missing argument for configure plan"};
+
+KFFT_API const char* kfft_strerr(const kfft_return_t code) {
+    if (code >= sizeof(kErrors) / sizeof(kErrors[0])) return "Unknown return code";
+    return kErrors[code];
+}
+
+KFFT_API void kfft_gb300_stats(kfft_gb300_stats_t* s) {
+    if (!s) return;
+    s->kernel_launches = g_launches.load();
+    s->graph_launches = g_graphs.load();
+    s->device_bytes = uint64_t(g_bytes.load());
+    s->device = g_device;
+    s->last_cuda_error = g_last_err.load();
+}
+
+KFFT_API const char* kfft_gb300_last_error(void) {
+    static thread_local std::string copy;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    copy = g_err_text;
+    return copy.c_str();
+}
+
+KFFT_API const char* kfft_gb300_describe(const kfft_plan_cpx* plan) {
+    static thread_local std::string s;
+    if (!plan || !plan->gpu || !plan->gpu->plan) s = "";
+    else s = describe(*plan->gpu->plan);
+    return s.c_str();
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// 2D complex and real (ext/2d/kfft_cpx2.c, ext/2d/kfft_scalar2.c)
+// ===========================================================================
+namespace {
+const FftPlan* gp(const kfft_plan_cpx* p) { return p && p->gpu ? p->gpu->plan : nullptr; }
+}  // namespace
+
+extern "C" {
+
+KFFT_API kfft_plan_c2d* kfft_config2_cpx(const uint32_t x_size, const uint32_t y_size,
+                                         const uint32_t flags, kfft_pool_t* A, size_t* lenmem) {
+    size_t memneed = sizeof(kfft_plan_c2d) + cpx_memneed(x_size) +
+                     (x_size != y_size ? cpx_memneed(y_size) : 0) + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_c2d* P = plan_prepare<kfft_plan_c2d>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = x_size * y_size;
+    P->x = x_size;
+    P->y = y_size;
+    P->flags = flags;
+    const uint32_t cf = KFFT_CHECK_FLAGS(flags);
+    P->plan_x = kfft_config_cpx(x_size, cf, mm, NULL);
+    P->plan_y = (x_size == y_size) ? P->plan_x : kfft_config_cpx(y_size, cf, mm, NULL);
+    if (!P->plan_x || !P->plan_y) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+}  // extern "C"
+
+namespace {
+// 2D complex transform on device buffers (rows of x, y rows)
+bool c2d_dev(const kfft_plan_c2d* p, const vec2_t* din, vec2_t* dout, Carve& cv, cudaStream_t st) {
+    const FftPlan* Px = gp(p->plan_x);
+    const FftPlan* Py = gp(p->plan_y);
+    if (!Px || !Py) return false;
+    const uint32_t x = p->x, y = p->y;
+    size_t wb = workspace_bytes(*Px, y);
+    void* w = cv.take(wb);
+    if (wb && !w) return false;
+    if (!run_cpx(*Px, din, dout, y, inverse_scale(p->flags, x), w, wb, st)) return false;
+    return run_columns(*Py, dout, x, y, inverse_scale(p->flags, y), cv, st);
+}
+
+size_t c2d_bytes(const kfft_plan_c2d* p) {
+    return r256(workspace_bytes(*gp(p->plan_x), p->y)) + columns_bytes(*gp(p->plan_y), p->x, p->y);
+}
+
+template <typename F>
+kfft_return_t with_staging(kfft_gpu_plan* g, size_t work, const void* const* ins,
+                           const size_t* in_bytes, int nin, void* out, size_t out_bytes, F&& body) {
+    cudaSetDevice(current_device());
+    cudaStream_t st = sync_stream();
+    bool hin[4] = {false, false, false, false};
+    size_t need = r256(work);
+    for (int i = 0; i < nin; ++i) {
+        hin[i] = !is_device_pointer(ins[i]);
+        if (hin[i]) need += r256(in_bytes[i]);
+    }
+    const bool hout = !is_device_pointer(out);
+    if (hout) need += r256(out_bytes);
+    Carve cv;
+    cv.base = static_cast<char*>(g->workspace(need));
+    cv.size = need;
+    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    const void* dins[4];
+    for (int i = 0; i < nin; ++i) {
+        if (hin[i]) {
+            void* s = cv.take(in_bytes[i]);
+            cudaMemcpyAsync(s, ins[i], in_bytes[i], cudaMemcpyHostToDevice, st);
+            dins[i] = s;
+        } else {
+            dins[i] = ins[i];
+        }
+    }
+    void* dout = hout ? cv.take(out_bytes) : out;
+    if (!body(dins, dout, cv, st)) return KFFT_RET_BUFFER_FAIL;
+    if (hout) cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, st);
+    return finish(st);
+}
+}  // namespace
+
+extern "C" {
+
+KFFT_API kfft_return_t kfft_eval2_cpx(kfft_plan_c2d* cfg, const kfft_cpx* fin, kfft_cpx* fout) {
+    if (!cfg || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (cfg->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = cfg->plan_x->gpu;
+    EvalGuard guard(g);
+    const size_t bytes = sizeof(vec2_t) * size_t(cfg->nfft);
+    const void* ins[1] = {fin};
+    return with_staging(g, c2d_bytes(cfg), ins, &bytes, 1, fout, bytes,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            return c2d_dev(cfg, static_cast<const vec2_t*>(di[0]),
+                                           static_cast<vec2_t*>(dout), cv, st);
+                        });
+}
+
+KFFT_API kfft_plan_s2d* kfft_config2_scalar(const uint32_t x_size, const uint32_t y_size,
+                                            const uint32_t flags, kfft_pool_t* A, size_t* lenmem) {
+    size_t rx = 0, ry = 0;
+    const uint32_t cf = KFFT_CHECK_FLAGS(flags);
+    // forward: real rows (expanded) + complex columns; inverse: complex rows + real columns
+    if (flags & KFFT_FLAG_INVERSE) {
+        rx = cpx_memneed(x_size);
+        ry = sizeof(kfft_plan_sclr) + cpx_memneed(y_size) + 2 * gpu_handle_bytes() + 32;
+    } else {
+        rx = sizeof(kfft_plan_sclr) + cpx_memneed(x_size) + 2 * gpu_handle_bytes() + 32;
+        ry = cpx_memneed(y_size);
+    }
+    size_t memneed = sizeof(kfft_plan_s2d) + rx + ry + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_s2d* P = plan_prepare<kfft_plan_s2d>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = x_size * y_size;
+    P->x = x_size;
+    P->y = y_size;
+    P->flags = flags;
+    if (flags & KFFT_FLAG_INVERSE) {
+        P->plan_x = reinterpret_cast<kfft_object_t*>(kfft_config_cpx(x_size, cf, mm, NULL));
+        P->plan_y = reinterpret_cast<kfft_object_t*>(
+            kfft_config_scalar(y_size, cf | KFFT_FLAG_EXPAND_SCALAR, mm, NULL));
+    } else {
+        P->plan_x = reinterpret_cast<kfft_object_t*>(
+            kfft_config_scalar(x_size, cf | KFFT_FLAG_EXPAND_SCALAR, mm, NULL));
+        P->plan_y = reinterpret_cast<kfft_object_t*>(kfft_config_cpx(y_size, cf, mm, NULL));
+    }
+    if (!P->plan_x || !P->plan_y) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+}  // extern "C"
+
+namespace {
+// real 2D forward on device: rows real (expanded) -> complex columns
+bool s2d_forward_dev(const kfft_plan_s2d* p, const real_t* din, vec2_t* dout, Carve& cv,
+                     cudaStream_t st) {
+    const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(p->plan_x);
+    const kfft_plan_cpx* cy = reinterpret_cast<const kfft_plan_cpx*>(p->plan_y);
+    if (!real_forward_dev(rx, din, dout, p->y, p->x, 1, cv, st)) return false;
+    return run_columns(*gp(cy), dout, p->x, p->y, real_t(1), cv, st);
+}
+size_t s2d_forward_bytes(const kfft_plan_s2d* p) {
+    const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(p->plan_x);
+    const kfft_plan_cpx* cy = reinterpret_cast<const kfft_plan_cpx*>(p->plan_y);
+    return real_forward_bytes(rx, p->y) + columns_bytes(*gp(cy), p->x, p->y);
+}
+// real 2D inverse on device: complex rows -> real columns (ext/2d/kfft_scalar2.c:185-246)
+bool s2d_inverse_dev(const kfft_plan_s2d* p, const vec2_t* din, real_t* dout, Carve& cv,
+                     cudaStream_t st) {
+    const kfft_plan_cpx* cx = reinterpret_cast<const kfft_plan_cpx*>(p->plan_x);
+    const kfft_plan_sclr* ry = reinterpret_cast<const kfft_plan_sclr*>(p->plan_y);
+    const uint32_t x = p->x, y = p->y;
+    const size_t n = size_t(x) * y;
+    vec2_t* rows = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * n));
+    vec2_t* cols = static_cast<vec2_t*>(cv.take(sizeof(vec2_t) * n));
+    real_t* rcols = static_cast<real_t*>(cv.take(sizeof(real_t) * n));
+    size_t wb = workspace_bytes(*gp(cx), y);
+    void* w = cv.take(wb);
+    if (!rows || !cols || !rcols || (wb && !w)) return false;
+    if (!run_cpx(*gp(cx), din, rows, y, inverse_scale(cx->flags, x), w, wb, st)) return false;
+    launch_transpose(rows, cols, y, x, 1, st);
+    if (!real_inverse_dev(ry, cols, y, rcols, x, cv, st)) return false;
+    launch_transpose_real(rcols, dout, x, y, st);
+    return true;
+}
+size_t s2d_inverse_bytes(const kfft_plan_s2d* p) {
+    const kfft_plan_cpx* cx = reinterpret_cast<const kfft_plan_cpx*>(p->plan_x);
+    const kfft_plan_sclr* ry = reinterpret_cast<const kfft_plan_sclr*>(p->plan_y);
+    const size_t n = size_t(p->x) * p->y;
+    return 2 * r256(sizeof(vec2_t) * n) + r256(sizeof(real_t) * n) +
+           r256(workspace_bytes(*gp(cx), p->y)) + real_inverse_bytes(ry, p->x);
+}
+kfft_gpu_plan* s2d_handle(const kfft_plan_s2d* p) {
+    if (p->flags & KFFT_FLAG_INVERSE)
+        return reinterpret_cast<const kfft_plan_cpx*>(p->plan_x)->gpu;
+    return reinterpret_cast<const kfft_plan_cpx*>(p->plan_y)->gpu;
+}
+}  // namespace
+
+extern "C" {
+
+KFFT_API kfft_return_t kfft_eval2_scalar(kfft_plan_s2d* plan, const kfft_scalar* fin,
+                                         kfft_cpx* fout) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->flags & KFFT_FLAG_INVERSE) return KFFT_RET_IMPROPER_PLAN;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = s2d_handle(plan);
+    EvalGuard guard(g);
+    const size_t ib = sizeof(real_t) * size_t(plan->nfft), ob = sizeof(vec2_t) * size_t(plan->nfft);
+    const void* ins[1] = {fin};
+    return with_staging(g, s2d_forward_bytes(plan), ins, &ib, 1, fout, ob,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            return s2d_forward_dev(plan, static_cast<const real_t*>(di[0]),
+                                                   static_cast<vec2_t*>(dout), cv, st);
+                        });
+}
+
+KFFT_API kfft_return_t kfft_evali2_scalar(kfft_plan_s2d* plan, const kfft_cpx* fin,
+                                          kfft_scalar* fout) {
+    if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
+    if (!(plan->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = s2d_handle(plan);
+    EvalGuard guard(g);
+    const size_t ib = sizeof(vec2_t) * size_t(plan->nfft), ob = sizeof(real_t) * size_t(plan->nfft);
+    const void* ins[1] = {fin};
+    return with_staging(g, s2d_inverse_bytes(plan), ins, &ib, 1, fout, ob,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            return s2d_inverse_dev(plan, static_cast<const vec2_t*>(di[0]),
+                                                   static_cast<real_t*>(dout), cv, st);
+                        });
+}
+
+// ===========================================================================
+// 1D convolution (ext/conv/kfft_cpx_conv.c, ext/conv/kfft_scalar_conv.c)
+// ===========================================================================
+KFFT_API kfft_plan_ccnv* kfft_config_conv_cpx(const uint32_t nfft, const uint32_t flags,
+                                              kfft_pool_t* A, size_t* lenmem) {
+    size_t memneed = sizeof(kfft_plan_ccnv) + 2 * cpx_memneed(nfft) + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_ccnv* P = plan_prepare<kfft_plan_ccnv>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = nfft;
+    P->flags = flags;
+    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
+    P->plan_fwd = kfft_config_cpx(nfft, cf, mm, NULL);
+    P->plan_inv = kfft_config_cpx(nfft, cf | KFFT_FLAG_INVERSE, mm, NULL);
+    if (!P->plan_fwd || !P->plan_inv) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_eval_conv_cpx(kfft_plan_ccnv* plan, const kfft_cpx* fin_A,
+                                          const kfft_cpx* fin_B, kfft_cpx* fout) {
+    if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->plan_fwd->gpu;
+    EvalGuard guard(g);
+    const FftPlan& F = *gp(plan->plan_fwd);
+    const FftPlan& I = *gp(plan->plan_inv);
+    const uint32_t n = plan->nfft;
+    const size_t bytes = sizeof(vec2_t) * size_t(n);
+    const size_t work = 2 * r256(bytes) + r256(std::max(workspace_bytes(F, 1), workspace_bytes(I, 1)));
+    const void* ins[2] = {fin_A, fin_B};
+    const size_t ibs[2] = {bytes, bytes};
+    return with_staging(g, work, ins, ibs, 2, fout, bytes,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            vec2_t* fa = static_cast<vec2_t*>(cv.take(bytes));
+                            vec2_t* fb = static_cast<vec2_t*>(cv.take(bytes));
+                            size_t wb = std::max(workspace_bytes(F, 1), workspace_bytes(I, 1));
+                            void* w = cv.take(wb);
+                            if (!fa || !fb || (wb && !w)) return false;
+                            if (!run_cpx(F, static_cast<const vec2_t*>(di[0]), fa, 1, real_t(1), w, wb, st))
+                                return false;
+                            if (!run_cpx(F, static_cast<const vec2_t*>(di[1]), fb, 1, real_t(1), w, wb, st))
+                                return false;
+                            launch_hadamard(fb, fa, n, st);
+                            return run_cpx(I, fb, static_cast<vec2_t*>(dout), 1,
+                                           inverse_scale(plan->plan_inv->flags, n), w, wb, st);
+                        });
+}
+
+KFFT_API kfft_plan_scnv* kfft_config_conv_scalar(const uint32_t nfft, const uint32_t flags,
+                                                 kfft_pool_t* A, size_t* lenmem) {
+    const uint32_t basis_n = (nfft % 2) ? nfft : nfft / 2;
+    size_t one = sizeof(kfft_plan_sclr) + cpx_memneed(basis_n) + gpu_handle_bytes() + 16;
+    size_t memneed = sizeof(kfft_plan_scnv) + 2 * one + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_scnv* P = plan_prepare<kfft_plan_scnv>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = nfft;
+    P->flags = flags;
+    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
+    P->plan_fwd = kfft_config_scalar(nfft, cf, mm, NULL);
+    P->plan_inv = kfft_config_scalar(nfft, cf | KFFT_FLAG_INVERSE, mm, NULL);
+    if (!P->plan_fwd || !P->plan_inv) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_eval_conv_scalar(kfft_plan_scnv* plan, const kfft_scalar* fin_A,
+                                             const kfft_scalar* fin_B, kfft_scalar* fout) {
+    if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->plan_fwd->basis->gpu;
+    EvalGuard guard(g);
+    const uint32_t n = plan->nfft;
+    const uint32_t bins = real_bins(plan->plan_fwd);
+    const size_t rb = sizeof(real_t) * size_t(n);
+    const size_t sb = sizeof(vec2_t) * size_t(bins);
+    const size_t work = 2 * r256(sb) + real_forward_bytes(plan->plan_fwd, 1) +
+                        real_inverse_bytes(plan->plan_inv, 1);
+    const void* ins[2] = {fin_A, fin_B};
+    const size_t ibs[2] = {rb, rb};
+    return with_staging(g, work, ins, ibs, 2, fout, rb,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            vec2_t* fa = static_cast<vec2_t*>(cv.take(sb));
+                            vec2_t* fb = static_cast<vec2_t*>(cv.take(sb));
+                            if (!fa || !fb) return false;
+                            int ex = (plan->plan_fwd->flags & KFFT_FLAG_EXPAND_SCALAR) ? 1 : 0;
+                            size_t mark = cv.used;
+                            if (!real_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[0]),
+                                                  fa, 1, bins, ex, cv, st))
+                                return false;
+                            cv.used = mark;
+                            if (!real_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[1]),
+                                                  fb, 1, bins, ex, cv, st))
+                                return false;
+                            cv.used = mark;
+                            launch_hadamard(fb, fa, bins, st);
+                            return real_inverse_dev(plan->plan_inv, fb, bins,
+                                                    static_cast<real_t*>(dout), 1, cv, st);
+                        });
+}
+
+// ===========================================================================
+// 2D convolution (ext/conv2d/kfft_cpx_conv.c, ext/conv2d/kfft_scalar_conv.c)
+// ===========================================================================
+KFFT_API kfft_plan_c2cnv* kfft_config2_conv_cpx(const uint32_t x, const uint32_t y,
+                                                const uint32_t flags, kfft_pool_t* A,
+                                                size_t* lenmem) {
+    size_t one = sizeof(kfft_plan_c2d) + cpx_memneed(x) + (x != y ? cpx_memneed(y) : 0) + 16;
+    size_t memneed = sizeof(kfft_plan_c2cnv) + 2 * one + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_c2cnv* P = plan_prepare<kfft_plan_c2cnv>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = x * y;
+    P->x = x;
+    P->y = y;  // the reference stores x here (ext/conv2d/kfft_cpx_conv.c:67); y is intended
+    P->flags = flags;
+    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
+    P->plan_fwd = kfft_config2_cpx(x, y, cf, mm, NULL);
+    P->plan_inv = kfft_config2_cpx(x, y, cf | KFFT_FLAG_INVERSE, mm, NULL);
+    if (!P->plan_fwd || !P->plan_inv) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_eval2_conv_cpx(kfft_plan_c2cnv* plan, const kfft_cpx* fin_A,
+                                           const kfft_cpx* fin_B, kfft_cpx* fout) {
+    if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = plan->plan_fwd->plan_x->gpu;
+    EvalGuard guard(g);
+    const size_t bytes = sizeof(vec2_t) * size_t(plan->nfft);
+    const size_t work = 2 * r256(bytes) + std::max(c2d_bytes(plan->plan_fwd), c2d_bytes(plan->plan_inv));
+    const void* ins[2] = {fin_A, fin_B};
+    const size_t ibs[2] = {bytes, bytes};
+    return with_staging(g, work, ins, ibs, 2, fout, bytes,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            vec2_t* fa = static_cast<vec2_t*>(cv.take(bytes));
+                            vec2_t* fb = static_cast<vec2_t*>(cv.take(bytes));
+                            if (!fa || !fb) return false;
+                            size_t mark = cv.used;
+                            if (!c2d_dev(plan->plan_fwd, static_cast<const vec2_t*>(di[0]), fa, cv, st))
+                                return false;
+                            cv.used = mark;
+                            if (!c2d_dev(plan->plan_fwd, static_cast<const vec2_t*>(di[1]), fb, cv, st))
+                                return false;
+                            cv.used = mark;
+                            launch_hadamard(fb, fa, plan->nfft, st);
+                            return c2d_dev(plan->plan_inv, fb, static_cast<vec2_t*>(dout), cv, st);
+                        });
+}
+
+KFFT_API kfft_plan_s2cnv* kfft_config2_conv_scalar(const uint32_t x, const uint32_t y,
+                                                   const uint32_t flags, kfft_pool_t* A,
+                                                   size_t* lenmem) {
+    size_t fwd = 0, inv = 0;
+    kfft_config2_scalar(x, y, KFFT_CHECK_FLAGS_CCNV(flags), NULL, &fwd);
+    kfft_config2_scalar(x, y, KFFT_CHECK_FLAGS_CCNV(flags) | KFFT_FLAG_INVERSE, NULL, &inv);
+    size_t memneed = sizeof(kfft_plan_s2cnv) + fwd + inv + 16;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_s2cnv* P = plan_prepare<kfft_plan_s2cnv>(flags, memneed, A, lenmem, &mm);
+    if (!P) return NULL;
+    P->nfft = x * y;
+    P->x = x;
+    P->y = y;
+    P->flags = flags;
+    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
+    P->plan_fwd = kfft_config2_scalar(x, y, cf, mm, NULL);
+    P->plan_inv = kfft_config2_scalar(x, y, cf | KFFT_FLAG_INVERSE, mm, NULL);
+    if (!P->plan_fwd || !P->plan_inv) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_eval2_conv_scalar(kfft_plan_s2cnv* plan, const kfft_scalar* fin_A,
+                                              const kfft_scalar* fin_B, kfft_scalar* fout) {
+    if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
+    if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    kfft_gpu_plan* g = s2d_handle(plan->plan_fwd);
+    EvalGuard guard(g);
+    const size_t n = plan->nfft;
+    const size_t rb = sizeof(real_t) * n, sb = sizeof(vec2_t) * n;
+    const size_t work = 2 * r256(sb) + std::max(s2d_forward_bytes(plan->plan_fwd),
+                                                s2d_inverse_bytes(plan->plan_inv));
+    const void* ins[2] = {fin_A, fin_B};
+    const size_t ibs[2] = {rb, rb};
+    return with_staging(g, work, ins, ibs, 2, fout, rb,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            vec2_t* fa = static_cast<vec2_t*>(cv.take(sb));
+                            vec2_t* fb = static_cast<vec2_t*>(cv.take(sb));
+                            if (!fa || !fb) return false;
+                            size_t mark = cv.used;
+                            if (!s2d_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[0]), fa, cv, st))
+                                return false;
+                            cv.used = mark;
+                            if (!s2d_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[1]), fb, cv, st))
+                                return false;
+                            cv.used = mark;
+                            launch_hadamard(fb, fa, n, st);
+                            return s2d_inverse_dev(plan->plan_inv, fb, static_cast<real_t*>(dout), cv, st);
+                        });
+}
+
+}  // extern "C"

@@ -1,0 +1,218 @@
+// engine.cuh -- internal interfaces of the GB300 FFT engine.
+//
+// A transform of length N is executed as a list of PassDesc records.  Each
+// pass is one Stockham step of radix R (R = a sub-FFT length that fits in one
+// CTA's shared memory) over a tile of C "lanes"; inside the CTA the length-R
+// sub-FFT itself runs as Stockham passes of small radices (2..16 and odd
+// primes up to 31) in shared memory.  Prime lengths become (p-1)-point cyclic
+// convolutions (Rader) or M-point chirp convolutions (Bluestein); both are
+// expressed as DIRECT sub-plans whose first/last passes carry fused
+// prologue/epilogue element operations, so every kernel launch of the engine
+// is one PassDesc (plus a few small elementwise kernels for the real
+// transform's post-twiddle and for transposes).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "kfft.h"
+
+namespace kfft {
+
+#if defined(KFFT_HALF_SCALAR)
+typedef float real_t;
+typedef float2 vec2_t;
+#else
+typedef double real_t;
+typedef double2 vec2_t;
+#endif
+
+// Largest radix handled inside a CTA by a dedicated butterfly.
+constexpr int kMaxInnerRadices = 12;
+// Largest prime factor a DIRECT plan accepts; larger primes go to Rader/Bluestein.
+constexpr uint32_t kMaxDirectPrime = 31;
+
+// ---- magic-number unsigned division, valid for every 32-bit numerator -----
+struct FastDiv {
+    uint32_t d;   // divisor
+    uint32_t m;   // magic multiplier
+    uint32_t s;   // shift
+    void init(uint32_t div);
+};
+
+enum : uint8_t { MODE_LANE = 0, MODE_ELEM = 1 };
+enum : uint8_t { ORDER_J = 0, ORDER_B = 1 };
+
+// Prologue: how a pass obtains input element n of sequence b.
+enum : uint8_t {
+    PRO_NONE = 0,   // in[b*bs + n*es]
+    PRO_CHIRP = 1,  // n < bound ? in[b*bs + n*es] * tab[n] : 0  (Bluestein pre-chirp + pad)
+    PRO_GATHER = 2, // in[b*bs + perm[n]*es]                    (Rader generator gather)
+};
+// Epilogue: how a pass stores output element k of sequence b.
+enum : uint8_t {
+    EPI_NONE = 0,      // out[b*bs + k*es] = v * scale
+    EPI_MUL = 1,       // out[b*bs + k*es] = v * tab[k]
+    EPI_CHIRP = 2,     // k < bound: out[b*bs + k*es] = v * tab[k] * scale
+    EPI_RADER_FWD = 3, // out[..k..] = v * tab[k]; k == 0: aux_out[2b] = x0, aux_out[2b+1] = x0 + v
+    EPI_RADER_INV = 4, // aux_out[b*bs + perm[k]*es] = (v + x0) * scale; k == 0 also X_0
+};
+
+struct PassDesc {
+    const vec2_t* in;
+    vec2_t* out;
+    uint64_t in_bs, out_bs;  // batch strides (elements)
+    uint32_t in_es, out_es;  // element strides
+    uint32_t batch;          // sequences
+    uint32_t N;              // transform length at this level
+    uint32_t R;              // sub-FFT length of this pass
+    uint32_t Ns;             // product of the lengths of the previous passes
+    uint32_t C;              // lanes per tile
+    uint32_t lanes_j;        // N / R
+    uint32_t tiles;          // ceil(batch * lanes_j / C)
+    uint32_t threads;        // CTA size
+    uint32_t smem_bytes;     // dynamic shared memory
+    uint8_t load_mode, store_mode, order;
+    uint8_t inv;             // butterfly direction (tables already carry it)
+    uint8_t nrad;
+    uint8_t rad[kMaxInnerRadices];
+    FastDiv div_R, div_lanes_j, div_batch, div_Ns, div_C;
+    const vec2_t* tw_inner;  // W_R^i, i < R
+    const vec2_t* tw_lo;     // W_N^i, i < 2^tw_shift
+    const vec2_t* tw_hi;     // W_N^(i << tw_shift)
+    uint32_t tw_shift;
+    uint32_t tw_mul;         // N / (Ns * R) = lanes_j / Ns
+    // fused element operations
+    uint8_t pro_op, epi_op;
+    const vec2_t* pro_tab;
+    const uint32_t* pro_perm;
+    uint32_t pro_bound;
+    const vec2_t* epi_tab;
+    const uint32_t* epi_perm;
+    uint32_t epi_bound;
+    const vec2_t* aux_in;   // Rader: the original input (x0)
+    vec2_t* aux_out;        // Rader: the final output
+    uint64_t aux_in_bs, aux_out_bs;
+    uint32_t aux_out_es;
+    real_t scale;
+};
+
+// ---- device tables -----------------------------------------------------
+// Fills t[i] = exp(sign * 2 pi i * (i * mult mod n) / n) in FP64 for i < count.
+void gen_twiddles(vec2_t* t, uint32_t count, uint64_t mult, uint32_t n, int sign,
+                  cudaStream_t st);
+// Bluestein chirp c[k] = exp(sign * i pi (k^2 mod 2n) / n), k < count.
+void gen_chirp(vec2_t* c, uint32_t count, uint32_t n, int sign, cudaStream_t st);
+// Bluestein filter b[m] = conj(c[|m|]) on the circle of m_len points (zero elsewhere).
+void gen_bluestein_filter(vec2_t* b, const vec2_t* chirp, uint32_t n, uint32_t m_len,
+                          cudaStream_t st);
+// Rader: s[j] = W_p^(pidx[j]) for j < p-1.
+void gen_rader_kernel(vec2_t* s, const uint32_t* pidx, uint32_t p, int sign, cudaStream_t st);
+// Real-transform post-twiddle table st[k] = exp(sign * i pi ((k+1)/h + 1/2)), k < h.
+void gen_super_twiddles(vec2_t* t, uint32_t h, int sign, cudaStream_t st);
+// Scale a table in place: t[i] *= s.
+void scale_table(vec2_t* t, uint32_t count, double s, cudaStream_t st);
+
+// ---- kernels run by the executor ------------------------------------------
+void launch_pass(const PassDesc& d, cudaStream_t st);
+// Even-N real transform post-processing (kfft_scalar.c:174-216): z holds the
+// N/2-point spectrum of each sequence, out gets nbins bins per sequence.
+void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32_t h,
+                      uint32_t batch, uint64_t out_bs, int expand, cudaStream_t st);
+// Even-N real inverse pre-processing (kfft_scalar.c:218-242).
+void launch_real_pre(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
+                     uint32_t batch, uint64_t in_bs, cudaStream_t st);
+// Odd-N helpers: real -> complex widening and complex -> real narrowing with scale.
+void launch_widen(const real_t* in, vec2_t* out, uint64_t n, cudaStream_t st);
+void launch_narrow(const vec2_t* in, real_t* out, uint64_t n, cudaStream_t st);
+// Batched out-of-place transpose of (rows x cols) matrices of complex / real.
+void launch_transpose(const vec2_t* in, vec2_t* out, uint32_t rows, uint32_t cols,
+                      uint32_t batch, cudaStream_t st);
+void launch_transpose_real(const real_t* in, real_t* out, uint32_t rows, uint32_t cols,
+                           cudaStream_t st);
+// b[i] *= a[i] (complex), i < n -- the Hadamard product of the convolutions.
+void launch_hadamard(vec2_t* b, const vec2_t* a, uint64_t n, cudaStream_t st);
+// Generic strided copy used for compaction (rows of `len` out of stride `src_stride`).
+void launch_copy_rows(const vec2_t* in, vec2_t* out, uint32_t len, uint64_t src_stride,
+                      uint64_t dst_stride, uint32_t rows, cudaStream_t st);
+
+// ---- host-side plan --------------------------------------------------------
+enum Method : uint32_t { METHOD_DIRECT = 0, METHOD_RADER = 1, METHOD_BLUESTEIN = 2 };
+
+struct PassSpec {
+    uint32_t R, Ns;
+    std::vector<uint8_t> radices;
+    const vec2_t* tw_inner;
+};
+
+struct DeviceArena;  // device memory owned by a plan tree
+
+struct FftPlan {
+    uint32_t N = 0;
+    int sign = -1;  // -1 forward, +1 inverse
+    Method method = METHOD_DIRECT;
+    // DIRECT
+    std::vector<PassSpec> passes;
+    const vec2_t* tw_lo = nullptr;
+    const vec2_t* tw_hi = nullptr;
+    uint32_t tw_shift = 0;
+    // RADER / BLUESTEIN: the convolution length and its two DIRECT sub-plans
+    uint32_t L = 0;
+    FftPlan* sub_fwd = nullptr;
+    FftPlan* sub_inv = nullptr;
+    const vec2_t* chirp = nullptr;   // Bluestein
+    const vec2_t* spectrum = nullptr; // Bluestein filter / Rader kernel spectrum, 1/L folded in
+    const uint32_t* gperm = nullptr;  // Rader: g^j mod p
+    const uint32_t* iperm = nullptr;  // Rader: g^-j mod p
+    uint32_t generator = 0;
+    ~FftPlan();
+};
+
+// Element layout of a batch of sequences.
+struct Layout {
+    uint32_t batch = 1;
+    uint64_t bs = 0;  // batch stride (elements)
+    uint32_t es = 1;  // element stride
+    uint8_t order = ORDER_J;
+};
+
+// Bump allocator over a caller-provided device workspace.
+struct Workspace {
+    char* base = nullptr;
+    size_t size = 0;
+    size_t used = 0;
+    vec2_t* take(size_t elems);
+};
+
+struct DeviceArena {
+    std::vector<void*> blocks;
+    size_t bytes = 0;
+    void* alloc(size_t bytes);
+    ~DeviceArena();
+};
+
+// Builds the plan of an N-point transform of direction `sign` on the current
+// device, allocating its tables from `arena`.  Returns nullptr on failure.
+FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st);
+bool is_direct_length(uint32_t n);
+std::string describe(const FftPlan& p);
+// Device workspace (bytes) the plan needs for `batch` sequences.
+size_t workspace_bytes(const FftPlan& p, uint32_t batch);
+// Appends the passes computing out = FFT(in) * scale to `descs`.
+bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t* out,
+                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
+void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
+
+// ---- runtime ----------------------------------------------------------------
+int current_device();
+bool ensure_device();
+void note_cuda_error(cudaError_t e);
+void count_launch(int64_t n = 1);
+void count_graph_launch();
+void account_device_bytes(int64_t delta);
+
+}  // namespace kfft

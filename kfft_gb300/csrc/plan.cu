@@ -1,0 +1,584 @@
+// plan.cu -- device planner and pass executor of the GB300 FFT engine.
+//
+// Replaces the reference planner (kf_factor / kfft_kinit / kfft_calculate,
+// kfft_cpx.c:103-318): instead of a recursive radix schedule with an N-entry
+// host twiddle table, a length N becomes
+//   DIRECT     N = R_0 * R_1 * ... (every prime factor <= 31): one Stockham
+//              pass per R_i, each R_i <= the shared-memory tile, FP64-generated
+//              device tables (W_R per pass, two-level W_N for the outer twiddles);
+//   RADER      N prime, N-1 DIRECT: (N-1)-point cyclic convolution with the
+//              generator gather fused into the first forward pass and the
+//              scatter into the last inverse pass (kfft_rader.c:17-63);
+//   BLUESTEIN  any other N: chirp-z convolution of length M >= 2N-1, M 7-smooth,
+//              with the chirps and the filter product fused into the passes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <sstream>
+
+#include "engine.cuh"
+
+namespace kfft {
+
+// ---------------------------------------------------------------------------
+// sizing rules
+// ---------------------------------------------------------------------------
+constexpr size_t kSmemBudget = 200 * 1024;  // bytes of dynamic shared memory per CTA
+#if defined(KFFT_HALF_SCALAR)
+constexpr uint32_t kPadShiftHost = 4;
+constexpr uint32_t kMultiLanes = 8;   // 64-byte row segments
+#else
+constexpr uint32_t kPadShiftHost = 3;
+constexpr uint32_t kMultiLanes = 4;   // 64-byte row segments
+#endif
+constexpr uint32_t kMultiRmax = 1024;
+
+static uint32_t pad_host(uint32_t i) { return i + (i >> kPadShiftHost); }
+
+static uint32_t tile_capacity() {
+    // two ping-pong buffers of pad(C*R)+1 elements
+    double per = 2.0 * sizeof(vec2_t) * (1.0 + 1.0 / double(1u << kPadShiftHost));
+    return uint32_t(double(kSmemBudget - 64) / per);
+}
+
+static uint32_t smem_for(uint32_t elems) {
+    return 2u * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
+}
+
+// ---------------------------------------------------------------------------
+// arithmetic helpers
+// ---------------------------------------------------------------------------
+static std::vector<uint32_t> prime_factors(uint32_t n) {
+    std::vector<uint32_t> f;
+    for (uint32_t p = 2; uint64_t(p) * p <= n; ++p)
+        while (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        }
+    if (n > 1) f.push_back(n);
+    return f;
+}
+
+bool is_direct_length(uint32_t n) {
+    if (n == 0) return false;
+    for (uint32_t p : prime_factors(n))
+        if (p > kMaxDirectPrime) return false;
+    return true;
+}
+
+static bool is_prime(uint32_t n) {
+    if (n < 2) return false;
+    for (uint32_t p = 2; uint64_t(p) * p <= n; ++p)
+        if (n % p == 0) return false;
+    return true;
+}
+
+static uint32_t modpow(uint64_t x, uint64_t y, uint64_t m) {
+    uint64_t r = 1 % m;
+    x %= m;
+    while (y) {
+        if (y & 1) r = r * x % m;
+        x = x * x % m;
+        y >>= 1;
+    }
+    return uint32_t(r);
+}
+
+// smallest primitive root of prime p (same choice as kfft_math.c:5-33)
+static uint32_t primitive_root(uint32_t p) {
+    std::vector<uint32_t> f = prime_factors(p - 1);
+    f.erase(std::unique(f.begin(), f.end()), f.end());
+    for (uint32_t g = 2; g < p; ++g) {
+        bool ok = true;
+        for (uint32_t q : f)
+            if (modpow(g, (p - 1) / q, p) == 1) {
+                ok = false;
+                break;
+            }
+        if (ok) return g;
+    }
+    return p == 2 ? 1 : 0;
+}
+
+// smallest 7-smooth integer >= n
+static uint64_t next_smooth(uint64_t n) {
+    uint64_t best = UINT64_MAX;
+    for (uint64_t a = 1; a < 2 * n + 2; a *= 2)
+        for (uint64_t b = a; b < 2 * n + 2; b *= 3)
+            for (uint64_t c = b; c < 2 * n + 2; c *= 5)
+                for (uint64_t d = c; d < 2 * n + 2; d *= 7)
+                    if (d >= n && d < best) best = d;
+    return best;
+}
+
+// inner radix schedule of a tile length R: 16s first, then 8/4/2, then odd primes
+static std::vector<uint8_t> inner_radices(uint32_t R) {
+    std::vector<uint8_t> r;
+    uint32_t e2 = 0;
+    while (R % 2 == 0) {
+        R /= 2;
+        ++e2;
+    }
+    while (e2 >= 4) {
+        r.push_back(16);
+        e2 -= 4;
+    }
+    if (e2 == 3) r.push_back(8);
+    if (e2 == 2) r.push_back(4);
+    if (e2 == 1) r.push_back(2);
+    for (uint32_t p : prime_factors(R)) r.push_back(uint8_t(p));
+    return r;
+}
+
+// split a DIRECT length into pass lengths, balanced, each <= rmax
+static std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
+    std::vector<uint32_t> f = prime_factors(N);
+    std::sort(f.rbegin(), f.rend());
+    for (uint32_t m = 1; m <= 32; ++m) {
+        std::vector<uint64_t> g(m, 1);
+        bool ok = true;
+        for (uint32_t p : f) {
+            // place in the group with the smallest product that still fits
+            int best = -1;
+            for (uint32_t i = 0; i < m; ++i)
+                if (g[i] * p <= rmax && (best < 0 || g[i] < g[best])) best = int(i);
+            if (best < 0) {
+                ok = false;
+                break;
+            }
+            g[best] *= p;
+        }
+        if (ok) {
+            std::vector<uint32_t> out;
+            for (uint64_t v : g)
+                if (v > 1) out.push_back(uint32_t(v));
+            std::sort(out.rbegin(), out.rend());
+            if (out.empty()) out.push_back(1);
+            return out;
+        }
+    }
+    return {};
+}
+
+// ---------------------------------------------------------------------------
+// device arena
+// ---------------------------------------------------------------------------
+void* DeviceArena::alloc(size_t n) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        return nullptr;
+    }
+    blocks.push_back(p);
+    bytes += n;
+    account_device_bytes(int64_t(n));
+    return p;
+}
+
+DeviceArena::~DeviceArena() {
+    for (void* p : blocks) cudaFree(p);
+    account_device_bytes(-int64_t(bytes));
+}
+
+vec2_t* Workspace::take(size_t elems) {
+    size_t bytes = (elems * sizeof(vec2_t) + 255) & ~size_t(255);
+    if (used + bytes > size) return nullptr;
+    vec2_t* p = reinterpret_cast<vec2_t*>(base + used);
+    used += bytes;
+    return p;
+}
+
+FftPlan::~FftPlan() {
+    delete sub_fwd;
+    delete sub_inv;
+}
+
+// ---------------------------------------------------------------------------
+// plan construction
+// ---------------------------------------------------------------------------
+static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
+    const uint32_t N = P->N;
+    std::vector<uint32_t> Rs;
+    if (N <= tile_capacity()) Rs.push_back(N);
+    else Rs = split_passes(N, kMultiRmax);
+    if (Rs.empty()) return false;
+    std::map<uint32_t, const vec2_t*> inner;
+    uint32_t Ns = 1;
+    for (uint32_t R : Rs) {
+        PassSpec s;
+        s.R = R;
+        s.Ns = Ns;
+        s.radices = inner_radices(R);
+        if (s.radices.size() > size_t(kMaxInnerRadices)) return false;
+        auto it = inner.find(R);
+        if (it == inner.end()) {
+            vec2_t* t = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * R));
+            if (!t) return false;
+            gen_twiddles(t, R, 1, R, P->sign, st);
+            it = inner.emplace(R, t).first;
+        }
+        s.tw_inner = it->second;
+        P->passes.push_back(s);
+        Ns *= R;
+    }
+    if (P->passes.size() > 1) {
+        uint32_t bits = 0;
+        while ((uint64_t(1) << bits) < N) ++bits;
+        uint32_t shift = (bits + 1) / 2;
+        uint32_t nlo = 1u << shift;
+        uint32_t nhi = (N >> shift) + 2;
+        vec2_t* lo = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * nlo));
+        vec2_t* hi = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * nhi));
+        if (!lo || !hi) return false;
+        gen_twiddles(lo, nlo, 1, N, P->sign, st);
+        gen_twiddles(hi, nhi, uint64_t(nlo), N, P->sign, st);
+        P->tw_lo = lo;
+        P->tw_hi = hi;
+        P->tw_shift = shift;
+    }
+    return true;
+}
+
+// runs `plan` once on device data to precompute a spectrum (contiguous, batch 1)
+static bool transform_once(const FftPlan& plan, const vec2_t* in, vec2_t* out, cudaStream_t st) {
+    size_t ws_bytes = workspace_bytes(plan, 1);
+    void* ws_mem = nullptr;
+    if (ws_bytes) {
+        cudaError_t e = cudaMalloc(&ws_mem, ws_bytes);
+        if (e != cudaSuccess) {
+            note_cuda_error(e);
+            return false;
+        }
+    }
+    Workspace ws;
+    ws.base = static_cast<char*>(ws_mem);
+    ws.size = ws_bytes;
+    Layout l;
+    l.batch = 1;
+    l.bs = plan.N;
+    std::vector<PassDesc> descs;
+    bool ok = build_passes(plan, in, l, out, l, real_t(1), ws, descs);
+    if (ok) run_passes(descs, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        ok = false;
+    }
+    if (ws_mem) cudaFree(ws_mem);
+    return ok;
+}
+
+FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st) {
+    FftPlan* P = new FftPlan();
+    P->N = N;
+    P->sign = sign;
+    if (N == 0) return P;
+    if (is_direct_length(N)) {
+        P->method = METHOD_DIRECT;
+        if (!build_direct(P, arena, st)) {
+            delete P;
+            return nullptr;
+        }
+        return P;
+    }
+    if (is_prime(N) && is_direct_length(N - 1)) {
+        // ---- Rader: X[g^-q] = x0 + sum_j x[g^j] W^(g^(j-q)) ------------------
+        P->method = METHOD_RADER;
+        const uint32_t L = N - 1;
+        P->L = L;
+        P->generator = primitive_root(N);
+        const uint32_t g = P->generator;
+        const uint32_t ginv = modpow(g, N - 2, N);
+        std::vector<uint32_t> gp(L), ip(L);
+        uint64_t a = 1, b = 1;
+        for (uint32_t j = 0; j < L; ++j) {
+            gp[j] = uint32_t(a);
+            ip[j] = uint32_t(b);
+            a = a * g % N;
+            b = b * ginv % N;
+        }
+        uint32_t* dgp = static_cast<uint32_t*>(arena.alloc(sizeof(uint32_t) * L));
+        uint32_t* dip = static_cast<uint32_t*>(arena.alloc(sizeof(uint32_t) * L));
+        vec2_t* kern = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * L));
+        vec2_t* spec = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * L));
+        if (!dgp || !dip || !kern || !spec) {
+            delete P;
+            return nullptr;
+        }
+        cudaMemcpyAsync(dgp, gp.data(), sizeof(uint32_t) * L, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dip, ip.data(), sizeof(uint32_t) * L, cudaMemcpyHostToDevice, st);
+        P->gperm = dgp;
+        P->iperm = dip;
+        P->sub_fwd = make_plan(L, -1, arena, st);
+        P->sub_inv = make_plan(L, +1, arena, st);
+        if (!P->sub_fwd || !P->sub_inv) {
+            delete P;
+            return nullptr;
+        }
+        // kernel s[j] = W_N^(g^-j) in the direction of the plan, spectrum / L
+        gen_rader_kernel(kern, dip, N, sign, st);
+        if (!transform_once(*P->sub_fwd, kern, spec, st)) {
+            delete P;
+            return nullptr;
+        }
+        scale_table(spec, L, 1.0 / double(L), st);
+        P->spectrum = spec;
+        return P;
+    }
+    // ---- Bluestein: X_k = c_k sum_n (x_n c_n) conj(c_{k-n}) --------------------
+    P->method = METHOD_BLUESTEIN;
+    uint64_t M = next_smooth(2 * uint64_t(N) - 1);
+    if (M > 0xFFFFFFFFull) {
+        delete P;
+        return nullptr;
+    }
+    P->L = uint32_t(M);
+    vec2_t* chirp = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * N));
+    vec2_t* filt = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * M));
+    vec2_t* spec = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * M));
+    if (!chirp || !filt || !spec) {
+        delete P;
+        return nullptr;
+    }
+    gen_chirp(chirp, N, N, sign, st);
+    gen_bluestein_filter(filt, chirp, N, uint32_t(M), st);
+    P->sub_fwd = make_plan(uint32_t(M), -1, arena, st);
+    P->sub_inv = make_plan(uint32_t(M), +1, arena, st);
+    if (!P->sub_fwd || !P->sub_inv) {
+        delete P;
+        return nullptr;
+    }
+    if (!transform_once(*P->sub_fwd, filt, spec, st)) {
+        delete P;
+        return nullptr;
+    }
+    scale_table(spec, uint32_t(M), 1.0 / double(M), st);
+    P->chirp = chirp;
+    P->spectrum = spec;
+    return P;
+}
+
+std::string describe(const FftPlan& p) {
+    std::ostringstream o;
+    const char* m[] = {"direct", "rader", "bluestein"};
+    o << "N=" << p.N << " " << m[p.method];
+    if (p.method != METHOD_DIRECT) {
+        o << " L=" << p.L << " [" << describe(*p.sub_fwd) << "]";
+        return o.str();
+    }
+    for (const PassSpec& s : p.passes) {
+        o << " | R=" << s.R << " Ns=" << s.Ns << " radices=";
+        for (size_t i = 0; i < s.radices.size(); ++i) o << (i ? "," : "") << int(s.radices[i]);
+    }
+    return o.str();
+}
+
+// ---------------------------------------------------------------------------
+// workspace and pass descriptors
+// ---------------------------------------------------------------------------
+static size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t workspace_bytes(const FftPlan& p, uint32_t batch) {
+    if (p.N == 0) return 0;
+    if (p.method == METHOD_DIRECT) {
+        size_t per = round256(sizeof(vec2_t) * size_t(p.N) * batch);
+        if (p.passes.size() >= 3) return 2 * per;
+        if (p.passes.size() == 2) return per;
+        return 0;
+    }
+    size_t a = round256(sizeof(vec2_t) * size_t(p.L) * batch);
+    size_t extra = (p.method == METHOD_RADER) ? round256(sizeof(vec2_t) * 2 * size_t(batch)) : 0;
+    return a + extra + std::max(workspace_bytes(*p.sub_fwd, batch), workspace_bytes(*p.sub_inv, batch));
+}
+
+struct Fuse {
+    uint8_t pro_op = PRO_NONE, epi_op = EPI_NONE;
+    const vec2_t* pro_tab = nullptr;
+    const uint32_t* pro_perm = nullptr;
+    uint32_t pro_bound = 0;
+    const vec2_t* epi_tab = nullptr;
+    const uint32_t* epi_perm = nullptr;
+    uint32_t epi_bound = 0;
+    const vec2_t* aux_in = nullptr;
+    vec2_t* aux_out = nullptr;
+    uint64_t aux_in_bs = 0, aux_out_bs = 0;
+    uint32_t aux_out_es = 1;
+};
+
+static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const Layout& lin,
+                          vec2_t* out, const Layout& lout, real_t scale) {
+    const PassSpec& s = P.passes[pi];
+    PassDesc d;
+    memset(&d, 0, sizeof(d));
+    d.in = in;
+    d.out = out;
+    d.in_bs = lin.bs;
+    d.out_bs = lout.bs;
+    d.in_es = lin.es;
+    d.out_es = lout.es;
+    d.batch = lin.batch;
+    d.N = P.N;
+    d.R = s.R;
+    d.Ns = s.Ns;
+    d.lanes_j = P.N / s.R;
+    d.order = lin.order;
+    d.inv = P.sign > 0 ? 1 : 0;
+    d.nrad = uint8_t(s.radices.size());
+    for (size_t i = 0; i < s.radices.size(); ++i) d.rad[i] = s.radices[i];
+    const uint32_t cap = tile_capacity();
+    uint32_t C;
+    if (d.order == ORDER_B) {
+        C = std::min<uint32_t>(16, std::max<uint32_t>(1, cap / s.R));
+        C = std::min(C, d.batch);
+        d.load_mode = MODE_LANE;
+        d.store_mode = MODE_LANE;
+    } else if (d.lanes_j == 1) {
+        const uint32_t target = (sizeof(vec2_t) == 8) ? 4096 : 2048;
+        C = std::max<uint32_t>(1, std::min(target / std::max<uint32_t>(s.R, 1), cap / std::max<uint32_t>(s.R, 1)));
+        C = std::min(C, d.batch);
+        d.load_mode = MODE_ELEM;
+        d.store_mode = MODE_ELEM;
+    } else {
+        C = std::min(kMultiLanes, d.lanes_j);
+        d.load_mode = MODE_LANE;
+        d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
+    }
+    if (C < 1) C = 1;
+    d.C = C;
+    const uint64_t lanes = uint64_t(d.batch) * d.lanes_j;
+    d.tiles = uint32_t((lanes + C - 1) / C);
+    uint32_t elems = C * s.R;
+    uint32_t t = (elems + 7) / 8;
+    t = (t + 31) / 32 * 32;
+    d.threads = std::max<uint32_t>(64, std::min<uint32_t>(512, t));
+    d.smem_bytes = smem_for(elems);
+    d.div_R.init(s.R);
+    d.div_lanes_j.init(d.lanes_j);
+    d.div_batch.init(d.batch);
+    d.div_Ns.init(s.Ns);
+    d.div_C.init(C);
+    d.tw_inner = s.tw_inner;
+    d.tw_lo = P.tw_lo;
+    d.tw_hi = P.tw_hi;
+    d.tw_shift = P.tw_shift;
+    d.tw_mul = d.lanes_j / s.Ns;
+    d.scale = scale;
+    return d;
+}
+
+static void apply_fuse(PassDesc& d, const Fuse& f, bool first, bool last) {
+    if (first) {
+        d.pro_op = f.pro_op;
+        d.pro_tab = f.pro_tab;
+        d.pro_perm = f.pro_perm;
+        d.pro_bound = f.pro_bound;
+    }
+    if (last) {
+        d.epi_op = f.epi_op;
+        d.epi_tab = f.epi_tab;
+        d.epi_perm = f.epi_perm;
+        d.epi_bound = f.epi_bound;
+        d.aux_in = f.aux_in;
+        d.aux_out = f.aux_out;
+        d.aux_in_bs = f.aux_in_bs;
+        d.aux_out_bs = f.aux_out_bs;
+        d.aux_out_es = f.aux_out_es;
+    }
+}
+
+static bool build_direct_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t* out,
+                                const Layout& lout, real_t scale, const Fuse& f, Workspace& ws,
+                                std::vector<PassDesc>& descs) {
+    const size_t m = P.passes.size();
+    if (m == 0) return true;
+    Layout mid;
+    mid.batch = lin.batch;
+    mid.order = lin.order;
+    if (lin.order == ORDER_B) {
+        mid.bs = 1;
+        mid.es = lin.batch;
+    } else {
+        mid.bs = P.N;
+        mid.es = 1;
+    }
+    vec2_t* s1 = nullptr;
+    vec2_t* s2 = nullptr;
+    if (m >= 2 && !(s1 = ws.take(size_t(P.N) * lin.batch))) return false;
+    if (m >= 3 && !(s2 = ws.take(size_t(P.N) * lin.batch))) return false;
+    const vec2_t* cur = in;
+    Layout lcur = lin;
+    for (size_t i = 0; i < m; ++i) {
+        const bool last = (i + 1 == m);
+        vec2_t* dst = last ? out : ((i % 2 == 0) ? s1 : s2);
+        Layout ldst = last ? lout : mid;
+        PassDesc d = make_desc(P, i, cur, lcur, dst, ldst, last ? scale : real_t(1));
+        apply_fuse(d, f, i == 0, last);
+        descs.push_back(d);
+        cur = dst;
+        lcur = ldst;
+    }
+    return true;
+}
+
+bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t* out,
+                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs) {
+    if (P.N == 0) return true;
+    if (uint64_t(lin.batch) * P.N >= (uint64_t(1) << 32) && P.method == METHOD_DIRECT &&
+        P.passes.size() > 1)
+        return false;  // lane indices are 32-bit
+    Fuse none;
+    if (P.method == METHOD_DIRECT) return build_direct_passes(P, in, lin, out, lout, scale, none, ws, descs);
+    if (lin.order != ORDER_J || lout.order != ORDER_J) return false;
+    const uint32_t B = lin.batch;
+    Layout la;
+    la.batch = B;
+    la.bs = P.L;
+    la.es = 1;
+    vec2_t* A = ws.take(size_t(P.L) * B);
+    if (!A) return false;
+    if (P.method == METHOD_BLUESTEIN) {
+        Fuse ff;
+        ff.pro_op = PRO_CHIRP;
+        ff.pro_tab = P.chirp;
+        ff.pro_bound = P.N;
+        ff.epi_op = EPI_MUL;
+        ff.epi_tab = P.spectrum;
+        Layout lx = lin;  // the input seen as length-L sequences with the caller's strides
+        if (!build_direct_passes(*P.sub_fwd, in, lx, A, la, real_t(1), ff, ws, descs)) return false;
+        Fuse fi;
+        fi.epi_op = EPI_CHIRP;
+        fi.epi_tab = P.chirp;
+        fi.epi_bound = P.N;
+        return build_direct_passes(*P.sub_inv, A, la, out, lout, scale, fi, ws, descs);
+    }
+    // Rader
+    vec2_t* pairs = ws.take(size_t(2) * B);
+    if (!pairs) return false;
+    Fuse ff;
+    ff.pro_op = PRO_GATHER;
+    ff.pro_perm = P.gperm;
+    ff.epi_op = EPI_RADER_FWD;
+    ff.epi_tab = P.spectrum;
+    ff.aux_in = in;
+    ff.aux_in_bs = lin.bs;
+    ff.aux_out = pairs;
+    if (!build_direct_passes(*P.sub_fwd, in, lin, A, la, real_t(1), ff, ws, descs)) return false;
+    Fuse fi;
+    fi.epi_op = EPI_RADER_INV;
+    fi.epi_perm = P.iperm;
+    fi.aux_in = pairs;
+    fi.aux_out = out;
+    fi.aux_out_bs = lout.bs;
+    fi.aux_out_es = lout.es;
+    return build_direct_passes(*P.sub_inv, A, la, A, la, scale, fi, ws, descs);
+}
+
+void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st) {
+    for (const PassDesc& d : descs) launch_pass(d, st);
+}
+
+}  // namespace kfft

@@ -1,0 +1,348 @@
+"""TEST INFRASTRUCTURE ONLY: numpy front end of the FP64 CPU oracle.
+
+The oracle (``kfft_oracle.c``) restates the reference kfft transform path in
+plain C.  This module compiles it with gcc when its shared object is missing
+and exposes numpy-level calls.  Only the tests, the smoke check and the CPU
+baseline leg of the benchmark import it; the product library never does.
+
+It also wraps the reference library itself (``oracle/_ref/libkfft_ref*.so``)
+when that was built by ``oracle/build_ref.sh`` (only possible where the
+reference sources are present), for pinning the oracle and for fixtures.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+SO_PATH = os.path.join(BUILD_DIR, "libkfft_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+FLAG_NORMAL = 0
+FLAG_INVERSE = 1 << 0
+FLAG_RENEW = 1 << 1
+FLAG_GENERIC = 1 << 2
+FLAG_GENERIC_ONLY = 1 << 3
+FLAG_EXPAND_SCALAR = 1 << 4
+FLAG_DISABLE_NORM = 1 << 5
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle C restatement into oracle/_build (gcc, OpenMP)."""
+    src = os.path.join(HERE, "kfft_oracle.c")
+    if (not force and os.path.exists(SO_PATH)
+            and os.path.getmtime(SO_PATH) >= os.path.getmtime(src)):
+        return SO_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = SO_PATH + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-std=gnu11", "-O3", "-fPIC", "-fopenmp", "-shared", "-o", tmp, src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, SO_PATH)
+    return SO_PATH
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        lib = ctypes.CDLL(build())
+        vp, u32, i32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64
+        lib.oracle_plan_cpx.restype = vp
+        lib.oracle_plan_cpx.argtypes = [u32, u32]
+        lib.oracle_plan_free.argtypes = [vp]
+        lib.oracle_exec_cpx_batch.argtypes = [vp, vp, vp, u64, i32]
+        for name in ("oracle_fft_cpx", "oracle_rfft", "oracle_irfft", "oracle_conv_cpx",
+                     "oracle_conv_scalar"):
+            getattr(lib, name).restype = i32
+        lib.oracle_fft_cpx.argtypes = [u32, u32, vp, vp]
+        lib.oracle_rfft.argtypes = [u32, u32, vp, vp]
+        lib.oracle_irfft.argtypes = [u32, u32, vp, vp]
+        lib.oracle_fft2_cpx.argtypes = [u32, u32, u32, vp, vp]
+        lib.oracle_rfft2.argtypes = [u32, u32, u32, vp, vp]
+        lib.oracle_irfft2.argtypes = [u32, u32, u32, vp, vp]
+        lib.oracle_conv_cpx.argtypes = [u32, u32, vp, vp, vp]
+        lib.oracle_conv_scalar.argtypes = [u32, u32, vp, vp, vp]
+        lib.oracle_conv2_cpx.argtypes = [u32, u32, u32, vp, vp, vp]
+        lib.oracle_conv2_scalar.argtypes = [u32, u32, u32, vp, vp, vp]
+        lib.oracle_dft_exact.argtypes = [u32, i32, vp, vp]
+        _lib = lib
+        return lib
+
+
+def _c128(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _check(r, what):
+    if r != 0:
+        raise RuntimeError(f"oracle {what} returned {r}")
+
+
+class CpxPlan:
+    """An oracle complex plan of one length, reusable over a batch."""
+
+    def __init__(self, nfft: int, flags: int = 0):
+        self.lib = _load()
+        self.nfft = nfft
+        self.ptr = self.lib.oracle_plan_cpx(nfft, flags)
+        if not self.ptr:
+            raise MemoryError("oracle plan allocation failed")
+
+    def __call__(self, x, threads: int = 0):
+        x = _c128(x)
+        batch = x.size // max(self.nfft, 1)
+        y = np.empty_like(x)
+        _check(self.lib.oracle_exec_cpx_batch(self.ptr, x.ctypes.data, y.ctypes.data,
+                                              batch, threads), "exec_cpx_batch")
+        return y
+
+    def close(self):
+        if self.ptr:
+            self.lib.oracle_plan_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fft_cpx(x, flags: int = 0):
+    """kfft_eval_cpx on one or more rows (last axis = sequence)."""
+    x = _c128(x)
+    n = x.shape[-1]
+    p = CpxPlan(n, flags)
+    try:
+        return p(x).reshape(x.shape)
+    finally:
+        p.close()
+
+
+def rfft(x, flags: int = 0):
+    lib = _load()
+    x = _f64(x)
+    n = x.size
+    out = np.zeros(n if (flags & FLAG_EXPAND_SCALAR or n % 2) else n // 2 + 1, np.complex128)
+    if n % 2 == 0 and not flags & FLAG_EXPAND_SCALAR:
+        buf = np.zeros(n // 2 + 1, np.complex128)
+    else:
+        buf = np.zeros(max(n, n // 2 + 1), np.complex128)
+    _check(lib.oracle_rfft(n, flags, x.ctypes.data, buf.ctypes.data), "rfft")
+    return buf[: out.size].copy()
+
+
+def irfft(X, n: int, flags: int = FLAG_INVERSE):
+    lib = _load()
+    X = _c128(X)
+    need = n if n % 2 else n // 2 + 1
+    if X.size < need:
+        raise ValueError("spectrum too short")
+    out = np.zeros(n + 2, np.float64)
+    _check(lib.oracle_irfft(n, flags, X.ctypes.data, out.ctypes.data), "irfft")
+    return out[:n].copy()
+
+
+def fft2_cpx(a, flags: int = 0):
+    """2D complex transform of a (y, x) row-major array (x contiguous)."""
+    lib = _load()
+    a = _c128(a)
+    y, x = a.shape
+    out = np.empty_like(a)
+    _check(lib.oracle_fft2_cpx(x, y, flags, a.ctypes.data, out.ctypes.data), "fft2_cpx")
+    return out
+
+
+def rfft2(a, flags: int = 0):
+    lib = _load()
+    a = _f64(a)
+    y, x = a.shape
+    out = np.zeros((y, x), np.complex128)
+    _check(lib.oracle_rfft2(x, y, flags, a.ctypes.data, out.ctypes.data), "rfft2")
+    return out
+
+
+def irfft2(A, flags: int = FLAG_INVERSE):
+    lib = _load()
+    A = _c128(A)
+    y, x = A.shape
+    out = np.zeros((y, x), np.float64)
+    _check(lib.oracle_irfft2(x, y, flags, A.ctypes.data, out.ctypes.data), "irfft2")
+    return out
+
+
+def conv_cpx(a, b, flags: int = 0):
+    lib = _load()
+    a, b = _c128(a), _c128(b)
+    out = np.empty_like(a)
+    _check(lib.oracle_conv_cpx(a.size, flags, a.ctypes.data, b.ctypes.data, out.ctypes.data),
+           "conv_cpx")
+    return out
+
+
+def conv_scalar(a, b, flags: int = 0):
+    lib = _load()
+    a, b = _f64(a), _f64(b)
+    out = np.zeros(a.size + 2, np.float64)
+    _check(lib.oracle_conv_scalar(a.size, flags, a.ctypes.data, b.ctypes.data,
+                                  out.ctypes.data), "conv_scalar")
+    return out[: a.size].copy()
+
+
+def conv2_cpx(a, b, flags: int = 0):
+    lib = _load()
+    a, b = _c128(a), _c128(b)
+    y, x = a.shape
+    out = np.empty_like(a)
+    _check(lib.oracle_conv2_cpx(x, y, flags, a.ctypes.data, b.ctypes.data, out.ctypes.data),
+           "conv2_cpx")
+    return out
+
+
+def conv2_scalar(a, b, flags: int = 0):
+    lib = _load()
+    a, b = _f64(a), _f64(b)
+    y, x = a.shape
+    out = np.zeros((y, x), np.float64)
+    _check(lib.oracle_conv2_scalar(x, y, flags, a.ctypes.data, b.ctypes.data,
+                                   out.ctypes.data), "conv2_scalar")
+    return out
+
+
+def dft_exact(x, inverse: bool = False):
+    """O(N^2) long-double DFT with integer phase reduction (small N only)."""
+    lib = _load()
+    x = _c128(x)
+    out = np.empty_like(x)
+    lib.oracle_dft_exact(x.size, int(inverse), x.ctypes.data, out.ctypes.data)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# The reference library itself (present only where oracle/build_ref.sh ran).
+# ---------------------------------------------------------------------------
+def ref_library_path(precision: str = "double") -> str | None:
+    name = {"double": "libkfft_ref.so", "float": "libkfft_ref_f.so",
+            "default": "libkfft_ref_default.so"}[precision]
+    p = os.path.join(REF_DIR, name)
+    if not os.path.exists(p):
+        return None
+    try:
+        ctypes.CDLL(p)
+    except OSError:
+        return None
+    return p
+
+
+class RefLib:
+    """ctypes view of the reference kfft C API (the upstream library built from source)."""
+
+    def __init__(self, precision: str = "double"):
+        path = ref_library_path(precision)
+        if path is None:
+            raise FileNotFoundError("reference library not built (oracle/build_ref.sh)")
+        self.lib = ctypes.CDLL(path)
+        self.real = np.float32 if precision == "float" else np.float64
+        self.cpx = np.complex64 if precision == "float" else np.complex128
+        vp, u32 = ctypes.c_void_p, ctypes.c_uint32
+        L = self.lib
+        for name in ("kfft_config_cpx", "kfft_config_scalar", "kfft_config_conv_cpx",
+                     "kfft_config_conv_scalar"):
+            getattr(L, name).restype = vp
+            getattr(L, name).argtypes = [u32, u32, vp, vp]
+        for name in ("kfft_config2_cpx", "kfft_config2_scalar", "kfft_config2_conv_cpx",
+                     "kfft_config2_conv_scalar"):
+            getattr(L, name).restype = vp
+            getattr(L, name).argtypes = [u32, u32, u32, vp, vp]
+        for name in ("kfft_eval_cpx", "kfft_eval_scalar", "kfft_evali_scalar", "kfft_eval2_cpx",
+                     "kfft_eval2_scalar", "kfft_evali2_scalar"):
+            getattr(L, name).argtypes = [vp, vp, vp]
+        for name in ("kfft_eval_conv_cpx", "kfft_eval_conv_scalar", "kfft_eval2_conv_cpx",
+                     "kfft_eval2_conv_scalar"):
+            getattr(L, name).argtypes = [vp, vp, vp, vp]
+        L.kfft_cleanup.argtypes = [vp]
+
+    def _run(self, cfg, args, ev, ins, out):
+        p = getattr(self.lib, cfg)(*args, None, None)
+        if not p:
+            raise MemoryError(cfg)
+        try:
+            r = getattr(self.lib, ev)(p, *[a.ctypes.data for a in ins], out.ctypes.data)
+        finally:
+            self.lib.kfft_cleanup(p)
+        if r != 0:
+            raise RuntimeError(f"{ev} returned {r}")
+        return out
+
+    def fft_cpx(self, x, flags=0):
+        x = np.ascontiguousarray(x, self.cpx)
+        return self._run("kfft_config_cpx", (x.size, flags), "kfft_eval_cpx", [x],
+                         np.empty_like(x))
+
+    def rfft(self, x, flags=0):
+        x = np.ascontiguousarray(x, self.real)
+        n = x.size
+        out = np.zeros(max(n, n // 2 + 1), self.cpx)
+        self._run("kfft_config_scalar", (n, flags), "kfft_eval_scalar", [x], out)
+        return out if (flags & FLAG_EXPAND_SCALAR or n % 2) else out[: n // 2 + 1].copy()
+
+    def irfft(self, X, n, flags=FLAG_INVERSE):
+        X = np.ascontiguousarray(X, self.cpx)
+        out = np.zeros(n + 2, self.real)
+        self._run("kfft_config_scalar", (n, flags), "kfft_evali_scalar", [X], out)
+        return out[:n].copy()
+
+    def fft2_cpx(self, a, flags=0):
+        a = np.ascontiguousarray(a, self.cpx)
+        y, x = a.shape
+        return self._run("kfft_config2_cpx", (x, y, flags), "kfft_eval2_cpx", [a],
+                         np.empty_like(a))
+
+    def rfft2(self, a, flags=0):
+        a = np.ascontiguousarray(a, self.real)
+        y, x = a.shape
+        return self._run("kfft_config2_scalar", (x, y, flags), "kfft_eval2_scalar", [a],
+                         np.zeros((y, x), self.cpx))
+
+    def irfft2(self, A, flags=FLAG_INVERSE):
+        A = np.ascontiguousarray(A, self.cpx)
+        y, x = A.shape
+        return self._run("kfft_config2_scalar", (x, y, flags), "kfft_evali2_scalar", [A],
+                         np.zeros((y, x), self.real))
+
+    def conv_cpx(self, a, b, flags=0):
+        a, b = (np.ascontiguousarray(v, self.cpx) for v in (a, b))
+        return self._run("kfft_config_conv_cpx", (a.size, flags), "kfft_eval_conv_cpx", [a, b],
+                         np.empty_like(a))
+
+    def conv_scalar(self, a, b, flags=0):
+        a, b = (np.ascontiguousarray(v, self.real) for v in (a, b))
+        out = np.zeros(a.size + 2, self.real)
+        self._run("kfft_config_conv_scalar", (a.size, flags), "kfft_eval_conv_scalar", [a, b],
+                  out)
+        return out[: a.size].copy()
+
+    def conv2_cpx(self, a, b, flags=0):
+        a, b = (np.ascontiguousarray(v, self.cpx) for v in (a, b))
+        y, x = a.shape
+        return self._run("kfft_config2_conv_cpx", (x, y, flags), "kfft_eval2_conv_cpx", [a, b],
+                         np.empty_like(a))
+
+    def conv2_scalar(self, a, b, flags=0):
+        a, b = (np.ascontiguousarray(v, self.real) for v in (a, b))
+        y, x = a.shape
+        return self._run("kfft_config2_conv_scalar", (x, y, flags), "kfft_eval2_conv_scalar",
+                         [a, b], np.zeros((y, x), self.real))

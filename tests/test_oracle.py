@@ -1,0 +1,123 @@
+"""The CPU oracle is pinned to the reference before anything is checked against it.
+
+* defs_cpx1.json: the reference unit-test golden ramps (test/unit/suites/defs_cpx1.h),
+  tolerance 1e-3 as in test/unit/suites/api_cpx1.c:10;
+* ref_vectors.npz: outputs of the reference double build on seeded inputs, every
+  transform family, generated by tests/golden/make_golden.py;
+* an exact long-double DFT and numpy.fft as independent checks.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import rel_l2, tol64
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_defs_cpx1_forward_and_inverse():
+    d = json.load(open(os.path.join(GOLD, "defs_cpx1.json")))
+    tol = d["tolerance"]
+    assert set(d["vectors"]) == {"2", "3", "5", "7", "330"}
+    for n, v in d["vectors"].items():
+        x = np.array([complex(*p) for p in v["in"]])
+        y = np.array([complex(*p) for p in v["out"]])
+        assert x.size == int(n)
+        out = O.fft_cpx(x)
+        assert np.max(np.abs(out.real - y.real)) <= tol and np.max(np.abs(out.imag - y.imag)) <= tol
+        back = O.fft_cpx(y, O.FLAG_INVERSE)
+        assert np.max(np.abs(back - x)) <= tol
+
+
+def test_ramp_closed_form():
+    # X_0 = N(N+1)/2, X_k = -N/2 + i (N/2) cot(pi k / N) for x[n] = n + 1
+    for n in (2, 3, 5, 7, 16, 330, 1000):
+        x = np.arange(1, n + 1, dtype=np.complex128)
+        k = np.arange(1, n)
+        ref = np.concatenate([[n * (n + 1) / 2], -n / 2 + 1j * (n / 2) / np.tan(np.pi * k / n)])
+        assert rel_l2(O.fft_cpx(x), ref) < 1e-13
+
+
+@pytest.mark.parametrize("kind", ["fwd", "inv", "invnn"])
+def test_complex_against_reference_fixtures(golden, kind):
+    flags = {"fwd": 0, "inv": O.FLAG_INVERSE, "invnn": O.FLAG_INVERSE | O.FLAG_DISABLE_NORM}[kind]
+    sizes = sorted(int(k.split("_")[-1]) for k in golden.files if k.startswith("cpx_in_"))
+    for n in sizes:
+        x = golden[f"cpx_in_{n}"]
+        assert rel_l2(O.fft_cpx(x, flags), golden[f"cpx_{kind}_{n}"]) <= tol64(n), n
+
+
+def test_real_against_reference_fixtures(golden):
+    sizes = sorted(int(k.split("_")[-1]) for k in golden.files if k.startswith("real_in_"))
+    for n in sizes:
+        x = golden[f"real_in_{n}"]
+        assert rel_l2(O.rfft(x), golden[f"real_fwd_{n}"]) <= tol64(n)
+        assert rel_l2(O.rfft(x, O.FLAG_EXPAND_SCALAR), golden[f"real_fwdx_{n}"]) <= tol64(n)
+        assert rel_l2(O.irfft(golden[f"real_spec_{n}"], n), golden[f"real_inv_{n}"]) <= tol64(n)
+
+
+def test_real_inverse_even_returns_twice_the_signal():
+    x = np.random.default_rng(3).uniform(-1, 1, 64)
+    assert rel_l2(O.irfft(np.fft.rfft(x), 64), 2 * x) < 1e-14
+    y = np.random.default_rng(4).uniform(-1, 1, 63)
+    assert rel_l2(O.irfft(np.fft.fft(y), 63), y) < 1e-14
+
+
+def test_2d_against_reference_fixtures(golden):
+    shapes = sorted({k.split("_")[-1] for k in golden.files if k.startswith("c2_in_")})
+    for s in shapes:
+        a = golden[f"c2_in_{s}"]
+        y, x = a.shape
+        t = tol64(x * y)
+        assert rel_l2(O.fft2_cpx(a), golden[f"c2_fwd_{s}"]) <= t
+        assert rel_l2(O.fft2_cpx(a, O.FLAG_INVERSE), golden[f"c2_inv_{s}"]) <= t
+        assert rel_l2(O.rfft2(golden[f"s2_in_{s}"]), golden[f"s2_fwd_{s}"]) <= t
+        assert rel_l2(O.irfft2(golden[f"s2_spec_{s}"]), golden[f"s2_inv_{s}"]) <= t
+        assert rel_l2(O.conv2_scalar(golden[f"s2_in_{s}"], golden[f"s2c_b_{s}"]),
+                      golden[f"s2c_out_{s}"]) <= t
+        if f"c2c_out_{s}" in golden.files:
+            assert rel_l2(O.conv2_cpx(a, golden[f"c2c_b_{s}"]), golden[f"c2c_out_{s}"]) <= t
+
+
+def test_conv_against_reference_fixtures(golden):
+    sizes = sorted(int(k.split("_")[-1]) for k in golden.files if k.startswith("cc_a_"))
+    for n in sizes:
+        a, b = golden[f"cc_a_{n}"], golden[f"cc_b_{n}"]
+        assert rel_l2(O.conv_cpx(a, b), golden[f"cc_out_{n}"]) <= tol64(n)
+        assert rel_l2(O.conv_scalar(a.real, b.real), golden[f"sc_out_{n}"]) <= tol64(n)
+
+
+def test_conv_is_circular():
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal(100) + 1j * rng.standard_normal(100)
+    b = rng.standard_normal(100) + 1j * rng.standard_normal(100)
+    ref = np.fft.ifft(np.fft.fft(a) * np.fft.fft(b))
+    assert rel_l2(O.conv_cpx(a, b), ref) < 1e-14
+
+
+def test_against_exact_dft_and_numpy():
+    rng = np.random.default_rng(6)
+    for n in (1, 2, 11, 25, 29, 97, 121, 169, 257, 331, 529):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        ex = O.dft_exact(x)
+        assert rel_l2(O.fft_cpx(x), ex) <= tol64(n)
+        assert rel_l2(np.fft.fft(x), ex) <= tol64(n)
+
+
+def test_2d_matches_numpy_layout():
+    rng = np.random.default_rng(7)
+    a = rng.standard_normal((6, 10)) + 1j * rng.standard_normal((6, 10))
+    assert rel_l2(O.fft2_cpx(a), np.fft.fft2(a)) < 1e-14
+
+
+def test_oracle_matches_built_reference_when_available():
+    if O.ref_library_path("double") is None:
+        pytest.skip("reference library not built here")
+    R = O.RefLib("double")
+    rng = np.random.default_rng(8)
+    for n in list(range(1, 80)) + [330, 1024, 2879, 4099, 65536]:
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        assert rel_l2(O.fft_cpx(x), R.fft_cpx(x)) <= tol64(n), n
