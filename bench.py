@@ -1,0 +1,485 @@
+"""Benchmark of the GB300 FFT engine (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload uneven|c2c4096]
+
+Metric: 5*N*log2(N) GFLOP/s summed over every transform of a step (forward and
+inverse counted separately), the reference's own throughput convention
+(test/bench/speed/*).  Workloads:
+
+* uneven (default): 4096 complex FP32 sequences in one launch, lengths
+  log-uniform in [16, 2^20] snapped to smooth / 11-13-smooth / prime classes,
+  ~2^28 points, re/im iid N(0,1), seed 2; one step = forward transform of the
+  whole batch.
+* c2c4096: 256 complex FP64 sequences of N = 4096, re/im iid U[-1,1), seed 1;
+  one step = forward + inverse.
+
+Inputs are resident in HBM for `value`; `e2e` goes through the C ABI with
+pinned host buffers (host->device and device->host copies inside the timed
+region).  The CPU baseline is the FP64 oracle port (the reference kfft
+algorithm restated in C, OpenMP over sequences) on this host's cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def _smooth_candidates(limit, primes):
+    vals = {1}
+    for p in primes:
+        new = set()
+        for v in vals:
+            x = v
+            while x <= limit:
+                new.add(x)
+                x *= p
+        vals = new
+    return np.array(sorted(vals))
+
+
+def _is_prime(n):
+    if n < 2:
+        return False
+    for p in range(2, int(math.isqrt(n)) + 1):
+        if n % p == 0:
+            return False
+    return True
+
+
+def uneven_lengths(seed=2, count=4096, lo=16, hi=1 << 20, target=1 << 28):
+    """Lengths of the uneven-batch workload: log-uniform, snapped by class."""
+    rng = np.random.default_rng(seed)
+    smooth = _smooth_candidates(hi, [2, 3, 5, 7])
+    s7 = smooth
+    with1113 = np.array(sorted({int(v * f) for v in s7 for f in (11, 13) if v * f <= hi}))
+    raw = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    cls = rng.permutation(np.array([0] * (count // 2) + [1] * (count // 4) +
+                                   [2] * (count - count // 2 - count // 4)))
+    out = []
+    for r, c in zip(raw, cls):
+        r = int(round(r))
+        if c == 0:
+            out.append(int(smooth[np.argmin(np.abs(smooth - r))]))
+        elif c == 1:
+            out.append(int(with1113[np.argmin(np.abs(with1113 - r))]))
+        else:
+            k = max(r, 17)
+            while not _is_prime(k):
+                k += 1
+            out.append(k)
+    out = np.array(out, dtype=np.int64)
+    # rescale to ~target points by dropping the largest sequences
+    order = np.argsort(out)
+    while out.sum() > target * 1.05 and len(out) > 1:
+        out = np.delete(out, np.argmax(out))
+    return out.astype(np.uint32)
+
+
+class Workload:
+    name = ""
+    precision = "double"
+
+    def flops_per_step(self) -> float:
+        raise NotImplementedError
+
+
+class C2C4096(Workload):
+    name = "c2c fp64 N=4096 batch 256 forward+inverse"
+    precision = "double"
+    N, B = 4096, 256
+
+    def __init__(self, lib):
+        self.lib = lib
+
+    def setup(self, torch, dev, nbuf):
+        rng = np.random.default_rng(1)
+        x = rng.uniform(-1, 1, (self.B, self.N)) + 1j * rng.uniform(-1, 1, (self.B, self.N))
+        self.host_in = x
+        self.fwd = self.lib.L.kfft_config_cpx(self.N, 0, None, None)
+        self.inv = self.lib.L.kfft_config_cpx(self.N, 1, None, None)
+        assert self.fwd and self.inv, self.lib.last_error()
+        # rotating input buffers: together larger than the 129 MB L2
+        self.ins = [torch.from_numpy(x).to(dev) for _ in range(nbuf)]
+        self.mid = torch.empty_like(self.ins[0])
+        self.out = torch.empty_like(self.ins[0])
+        self.pin_in = torch.from_numpy(x).pin_memory()
+        self.pin_mid = torch.empty_like(self.pin_in).pin_memory()
+        self.pin_out = torch.empty_like(self.pin_in).pin_memory()
+
+    def bytes_per_buffer(self):
+        return self.N * self.B * 16
+
+    def flops_per_step(self):
+        return 2 * 5.0 * self.N * math.log2(self.N) * self.B
+
+    def launches_per_step(self):
+        return 2
+
+    def algorithmic_bytes_per_launch(self):
+        return 2 * self.N * self.B * 16  # read once, write once
+
+    def step(self, i, stream):
+        L = self.lib.L
+        x = self.ins[i % len(self.ins)]
+        s = ctypes.c_void_p(stream)
+        r1 = L.kfft_eval_cpx_async(self.fwd, x.data_ptr(), self.mid.data_ptr(), self.B, s)
+        r2 = L.kfft_eval_cpx_async(self.inv, self.mid.data_ptr(), self.out.data_ptr(), self.B, s)
+        assert r1 == 0 and r2 == 0
+
+    def step_e2e(self):
+        L = self.lib.L
+        r1 = L.kfft_eval_cpx_batch(self.fwd, self.pin_in.data_ptr(), self.pin_mid.data_ptr(), self.B)
+        r2 = L.kfft_eval_cpx_batch(self.inv, self.pin_mid.data_ptr(), self.pin_out.data_ptr(), self.B)
+        assert r1 == 0 and r2 == 0
+
+    def e2e_bytes(self):
+        b = self.N * self.B * 16
+        return 2 * b, 2 * b
+
+    def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
+        fwd = oracle_mod.CpxPlan(self.N, 0)
+        inv = oracle_mod.CpxPlan(self.N, 1)
+        x = self.host_in
+        n_done, t0 = 0, time.perf_counter()
+        while True:
+            y = fwd(x, threads)
+            inv(y, threads)
+            n_done += 1
+            el = time.perf_counter() - t0
+            if el > budget_s:
+                break
+        fwd.close()
+        inv.close()
+        return self.flops_per_step() * n_done / el / 1e9, f"{n_done} steps of the full workload"
+
+    def check(self):
+        from oracle import oracle
+        y = self.out.cpu().numpy()
+        return float(np.linalg.norm(y - self.host_in) / np.linalg.norm(self.host_in))
+
+
+class Uneven(Workload):
+    precision = "float"
+
+    def __init__(self, lib, precision="float"):
+        self.lib = lib
+        self.precision = precision
+        self.lengths = uneven_lengths()
+        self.total = int(self.lengths.sum(dtype=np.int64))
+        self.name = (f"uneven batch: {len(self.lengths)} complex {'fp32' if precision == 'float' else 'fp64'}"
+                     f" sequences, lengths log-uniform in [16, 2^20], {self.total} points, forward")
+
+    def setup(self, torch, dev, nbuf):
+        cdt = torch.complex64 if self.precision == "float" else torch.complex128
+        g = torch.Generator(device="cpu").manual_seed(2)
+        re = torch.randn(self.total, generator=g)
+        im = torch.randn(self.total, generator=g)
+        x = torch.complex(re, im).to(cdt)
+        self.host_in = x
+        self.plan = self.lib.L.kfft_config_cpx_uneven(len(self.lengths), self.lengths.ctypes.data, 0)
+        assert self.plan, self.lib.last_error()
+        self.ins = [x.to(dev)]
+        self.out = torch.empty_like(self.ins[0])
+        self.pin_in = x.pin_memory()
+        self.pin_out = torch.empty_like(x).pin_memory()
+
+    def flops_per_step(self):
+        n = self.lengths.astype(np.float64)
+        return float(np.sum(5.0 * n * np.log2(np.maximum(n, 2))))
+
+    def launches_per_step(self):
+        return None
+
+    def algorithmic_bytes_per_launch(self):
+        return None
+
+    def step(self, i, stream):
+        r = self.lib.L.kfft_eval_cpx_uneven_async(self.plan, self.ins[0].data_ptr(),
+                                                  self.out.data_ptr(), ctypes.c_void_p(stream))
+        assert r == 0, self.lib.last_error()
+
+    def step_e2e(self):
+        r = self.lib.L.kfft_eval_cpx_uneven(self.plan, self.pin_in.data_ptr(), self.pin_out.data_ptr())
+        assert r == 0
+
+    def e2e_bytes(self):
+        b = self.total * (8 if self.precision == "float" else 16)
+        return b, b
+
+    def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
+        # bounded sample: every 16th sequence, timed until the budget is spent
+        idx = np.arange(0, len(self.lengths), 16)
+        offs = np.concatenate([[0], np.cumsum(self.lengths.astype(np.int64))])
+        x = self.host_in.numpy().astype(np.complex128)
+        flops, t0, done = 0.0, time.perf_counter(), 0
+        plans = {}
+        while time.perf_counter() - t0 < budget_s:
+            for i in idx:
+                n = int(self.lengths[i])
+                p = plans.get(n) or plans.setdefault(n, oracle_mod.CpxPlan(n, 0))
+                p(x[offs[i]:offs[i] + n], threads)
+                flops += 5.0 * n * math.log2(max(n, 2))
+                if time.perf_counter() - t0 > budget_s:
+                    break
+            done += 1
+        el = time.perf_counter() - t0
+        for p in plans.values():
+            p.close()
+        return flops / el / 1e9, f"every 16th sequence ({len(idx)} of {len(self.lengths)}), {el:.1f}s"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args, ws, rank):
+    """The reference algorithm on the host cores (oracle port), same metric."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    import kfft_gb300  # noqa: F401  (only for the workload definitions' library arg)
+
+    class _NoLib:
+        L = None
+    wl = make_workload(args.workload, _NoLib(), need_lib=False)
+    threads = os.cpu_count() or 1
+    if isinstance(wl, Uneven):
+        g = np.random.default_rng(2)
+        x = (g.standard_normal(wl.total) + 1j * g.standard_normal(wl.total)).astype(np.complex64)
+        import types
+        wl.host_in = types.SimpleNamespace(numpy=lambda: x)
+    else:
+        rng = np.random.default_rng(1)
+        wl.host_in = rng.uniform(-1, 1, (wl.B, wl.N)) + 1j * rng.uniform(-1, 1, (wl.B, wl.N))
+    budget = max(2.0, 20.0 / max(args.steps + args.warmup, 1))
+    vals, samples = [], []
+    for _ in range(args.warmup):
+        wl.cpu_sample(oracle, threads, budget_s=budget / 2)
+    for _ in range(args.steps):
+        v, s = wl.cpu_sample(oracle, threads, budget_s=budget)
+        vals.append(v)
+        samples.append(s)
+    v = statistics.median(vals)
+    ms = wl.flops_per_step() / (v * 1e9) * 1e3
+    line = {"impl": "reference", "metric": "5N*log2N GFLOP/s", "value": round(v, 3),
+            "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl.name, "implementation": "reference kfft algorithm (FP64 C oracle port), OpenMP over sequences"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads,
+                             "kind": "port", "sample": samples[0]},
+            "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def make_workload(name, lib, need_lib=True):
+    if name == "c2c4096":
+        return C2C4096(lib)
+    return Uneven(lib)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("KFFT_BENCH_WORKLOAD", "uneven"),
+                    choices=["uneven", "c2c4096"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import kfft_gb300
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    probe = make_workload(args.workload, None)
+    lib = kfft_gb300.load(probe.precision)
+    wl = make_workload(args.workload, lib)
+    nbuf = 1
+    if hasattr(wl, "bytes_per_buffer"):
+        nbuf = max(1, int(math.ceil(268e6 / wl.bytes_per_buffer())))
+    wl.setup(torch, dev, nbuf)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            wl.step(i, sptr)
+    stream.synchronize()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.stats().kernel_launches
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        start.record(stream)
+        for i in range(args.steps):
+            wl.step(i, sptr)
+        end.record(stream)
+        end.synchronize()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    launches = lib.stats().kernel_launches - l0
+    ms_total = start.elapsed_time(end)
+    if pg:
+        t = torch.tensor([ms_total], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms = ms_total / args.steps
+    value = ws * wl.flops_per_step() / (ms / 1e3) / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    for _ in range(2):
+        wl.step_e2e()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        wl.step_e2e()
+    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+    h2d, d2h = wl.e2e_bytes()
+    e2e_val = ws * wl.flops_per_step() / (e2e_ms / 1e3) / 1e9
+
+    peak, peak_kind = measured_peaks()
+    roof = dominant_kernel_roofline(wl, ms, lib, peak, peak_kind)
+    line = {"metric": "5N*log2N GFLOP/s", "value": round(value, 2), "unit": "GFLOP/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if wl.precision == "float" else "f64",
+            "data": "synthetic",
+            "config": {"workload": wl.name, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs rotate over buffers larger than the 129 MB L2"
+                       if nbuf > 1 else "working set larger than the 129 MB L2"},
+            "e2e": {"value": round(e2e_val, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
+            "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle
+        threads = os.cpu_count() or 1
+        v, sample = wl.cpu_sample(oracle, threads)
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads,
+                                "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind):
+    per = wl.algorithmic_bytes_per_launch()
+    n = wl.launches_per_step()
+    if per is None or not n:
+        total_bytes = wl.total * (8 if wl.precision == "float" else 16) * 2
+        achieved = total_bytes / (ms_step / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "peak_source": peak_kind, "kernel": "k_pass (all passes of the batch)"}
+    dur = ms_step / n
+    achieved = per / (dur / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+            "kernel": "k_pass", "launch_ms": round(dur, 4)}
+
+
+if __name__ == "__main__":
+    main()

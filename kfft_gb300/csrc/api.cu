@@ -42,8 +42,11 @@ void count_launch(int64_t n) { g_launches += uint64_t(n); }
 void count_graph_launch() { g_graphs += 1; }
 void account_device_bytes(int64_t d) { g_bytes += d; }
 
+static thread_local int t_pending = 0;
+
 void note_cuda_error(cudaError_t e) {
     if (e == cudaSuccess) return;
+    t_pending = int(e);
     g_last_err = int(e);
     std::lock_guard<std::mutex> lk(g_err_mu);
     g_err_text = cudaGetErrorString(e);
@@ -69,6 +72,12 @@ bool ensure_device() {
 }
 
 int current_device() { return g_device; }
+
+int take_pending_error() {
+    int e = t_pending;
+    t_pending = 0;
+    return e;
+}
 }  // namespace kfft
 
 // ===========================================================================
@@ -158,11 +167,9 @@ cudaStream_t sync_stream() { return cudaStreamPerThread; }
 kfft_return_t finish(cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        note_cuda_error(e);
-        return KFFT_RET_BUFFER_FAIL;
-    }
-    return KFFT_RET_SUCCESS;
+    if (e != cudaSuccess) note_cuda_error(e);
+    const int pending = take_pending_error();
+    return pending ? KFFT_RET_BUFFER_FAIL : KFFT_RET_SUCCESS;
 }
 
 real_t inverse_scale(uint32_t flags, uint32_t n) {
@@ -449,12 +456,7 @@ KFFT_API kfft_return_t kfft_eval_cpx_async(kfft_plan_cpx* plan, const kfft_cpx* 
     if (!run_cpx(P, reinterpret_cast<const vec2_t*>(fin), reinterpret_cast<vec2_t*>(fout), batch,
                  inverse_scale(plan->flags, plan->nfft), w, wsb, st))
         return KFFT_RET_BUFFER_FAIL;
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        note_cuda_error(e);
-        return KFFT_RET_BUFFER_FAIL;
-    }
-    return KFFT_RET_SUCCESS;
+    return take_pending_error() ? KFFT_RET_BUFFER_FAIL : KFFT_RET_SUCCESS;
 }
 
 // ===========================================================================

@@ -33,6 +33,8 @@ typedef double2 vec2_t;
 
 // Largest radix handled inside a CTA by a dedicated butterfly.
 constexpr int kMaxInnerRadices = 12;
+// CTA size ceiling of the pass kernels (their register budget is sized for it).
+constexpr uint32_t kPassThreads = 256;
 // Largest prime factor a DIRECT plan accepts; larger primes go to Rader/Bluestein.
 constexpr uint32_t kMaxDirectPrime = 31;
 
@@ -119,6 +121,15 @@ void scale_table(vec2_t* t, uint32_t count, double s, cudaStream_t st);
 
 // ---- kernels run by the executor ------------------------------------------
 void launch_pass(const PassDesc& d, cudaStream_t st);
+// Persistent work-queue execution of many pass chains in one launch: `items`
+// lists (desc, tile) pairs ordered by dependency level; deps[d] is the pass
+// that must finish before any tile of pass d starts (-1: none).  A bounded wait
+// that gives up sets *error instead of hanging.  Radices must be <= 16.
+size_t pass_extra_bytes();
+void fill_extras(const PassDesc* d, void* extras, size_t n);
+bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
+                       const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
+                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st);
 // Even-N real transform post-processing (kfft_scalar.c:174-216): z holds the
 // N/2-point spectrum of each sequence, out gets nbins bins per sequence.
 void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32_t h,
@@ -197,8 +208,9 @@ struct DeviceArena {
 
 // Builds the plan of an N-point transform of direction `sign` on the current
 // device, allocating its tables from `arena`.  Returns nullptr on failure.
-FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st);
-bool is_direct_length(uint32_t n);
+FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
+                   uint32_t max_prime = kMaxDirectPrime);
+bool is_direct_length(uint32_t n, uint32_t max_prime = kMaxDirectPrime);
 std::string describe(const FftPlan& p);
 // Device workspace (bytes) the plan needs for `batch` sequences.
 size_t workspace_bytes(const FftPlan& p, uint32_t batch);
@@ -211,6 +223,8 @@ void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
 int current_device();
 bool ensure_device();
 void note_cuda_error(cudaError_t e);
+// returns and clears the CUDA error recorded on this host thread since the last call
+int take_pending_error();
 void count_launch(int64_t n = 1);
 void count_graph_launch();
 void account_device_bytes(int64_t delta);

@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
+
 #include "engine.cuh"
 
 namespace kfft {
@@ -309,9 +311,19 @@ __device__ __forceinline__ void inner_pass(const vec2_t* __restrict__ src, vec2_
     }
 }
 
-template <bool INV>
+template <bool INV, bool BIG>
 __device__ __forceinline__ void run_inner(int P, const vec2_t* src, vec2_t* dst, uint32_t R,
                                           uint32_t C, const InnerStep& st, const vec2_t* tw) {
+    if constexpr (BIG) {
+        switch (P) {
+            case 17: inner_pass<17, INV>(src, dst, R, C, st, tw); return;
+            case 19: inner_pass<19, INV>(src, dst, R, C, st, tw); return;
+            case 23: inner_pass<23, INV>(src, dst, R, C, st, tw); return;
+            case 29: inner_pass<29, INV>(src, dst, R, C, st, tw); return;
+            case 31: inner_pass<31, INV>(src, dst, R, C, st, tw); return;
+            default: break;
+        }
+    }
     switch (P) {
         case 2: inner_pass<2, INV>(src, dst, R, C, st, tw); break;
         case 3: inner_pass<3, INV>(src, dst, R, C, st, tw); break;
@@ -322,11 +334,6 @@ __device__ __forceinline__ void run_inner(int P, const vec2_t* src, vec2_t* dst,
         case 11: inner_pass<11, INV>(src, dst, R, C, st, tw); break;
         case 13: inner_pass<13, INV>(src, dst, R, C, st, tw); break;
         case 16: inner_pass<16, INV>(src, dst, R, C, st, tw); break;
-        case 17: inner_pass<17, INV>(src, dst, R, C, st, tw); break;
-        case 19: inner_pass<19, INV>(src, dst, R, C, st, tw); break;
-        case 23: inner_pass<23, INV>(src, dst, R, C, st, tw); break;
-        case 29: inner_pass<29, INV>(src, dst, R, C, st, tw); break;
-        case 31: inner_pass<31, INV>(src, dst, R, C, st, tw); break;
         default: break;
     }
 }
@@ -335,12 +342,12 @@ __device__ __forceinline__ vec2_t load_elem(const PassDesc& d, uint32_t b, uint3
     switch (d.pro_op) {
         case PRO_CHIRP:
             if (n < d.pro_bound)
-                return cmul(d.in[b * d.in_bs + uint64_t(n) * d.in_es], __ldg(&d.pro_tab[n]));
+                return cmul(__ldcg(&d.in[b * d.in_bs + uint64_t(n) * d.in_es]), __ldg(&d.pro_tab[n]));
             return {real_t(0), real_t(0)};
         case PRO_GATHER:
-            return d.in[b * d.in_bs + uint64_t(__ldg(&d.pro_perm[n])) * d.in_es];
+            return __ldcg(&d.in[b * d.in_bs + uint64_t(__ldg(&d.pro_perm[n])) * d.in_es]);
         default:
-            return d.in[b * d.in_bs + uint64_t(n) * d.in_es];
+            return __ldcg(&d.in[b * d.in_bs + uint64_t(n) * d.in_es]);
     }
 }
 
@@ -359,7 +366,7 @@ __device__ __forceinline__ void store_elem(const PassDesc& d, uint32_t b, uint32
             // is sum_{n>=1} x_n, so X_0 = x_0 + v is saved with x_0 per sequence
             d.out[b * d.out_bs + uint64_t(k) * d.out_es] = cmul(v, __ldg(&d.epi_tab[k]));
             if (k == 0) {
-                const vec2_t x0 = d.aux_in[b * d.aux_in_bs];
+                const vec2_t x0 = __ldcg(&d.aux_in[b * d.aux_in_bs]);
                 d.aux_out[2 * uint64_t(b)] = x0;
                 d.aux_out[2 * uint64_t(b) + 1] = cadd(x0, v);
             }
@@ -367,11 +374,11 @@ __device__ __forceinline__ void store_elem(const PassDesc& d, uint32_t b, uint32
         case EPI_RADER_INV: {
             // X[g^-k] = x_0 + c_k, and X_0 from the saved pair; never reads the input,
             // so the transform may run in place
-            const vec2_t x0 = d.aux_in[2 * uint64_t(b)];
+            const vec2_t x0 = __ldcg(&d.aux_in[2 * uint64_t(b)]);
             const uint32_t idx = __ldg(&d.epi_perm[k]);
             vec2_t* o = d.aux_out + b * d.aux_out_bs;
             o[uint64_t(idx) * d.aux_out_es] = cscale(cadd(v, x0), d.scale);
-            if (k == 0) o[0] = cscale(d.aux_in[2 * uint64_t(b) + 1], d.scale);
+            if (k == 0) o[0] = cscale(__ldcg(&d.aux_in[2 * uint64_t(b) + 1]), d.scale);
             break;
         }
         default:
@@ -384,14 +391,16 @@ struct PassExtra {
     InnerStep step[kMaxInnerRadices];
 };
 
-template <bool INV>
-__global__ void k_pass(const __grid_constant__ PassDesc d, const __grid_constant__ PassExtra x) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    vec2_t* bufA = reinterpret_cast<vec2_t*>(smem_raw);
+PassExtra make_extra(const PassDesc& d);
+
+// One tile of one pass: C lanes of the length-R sub-FFT, shared-memory staged.
+template <bool INV, bool BIG>
+__device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x, uint32_t tile,
+                                          vec2_t* bufA) {
     const uint32_t tile_elems = d.C * d.R;
     vec2_t* bufB = bufA + pad(tile_elems) + 1;
     const uint32_t total_lanes = d.batch * d.lanes_j;
-    const uint32_t lane0 = blockIdx.x * d.C;
+    const uint32_t lane0 = tile * d.C;
 
     // ---- load -----------------------------------------------------------
     for (uint32_t idx = threadIdx.x; idx < tile_elems; idx += blockDim.x) {
@@ -432,7 +441,7 @@ __global__ void k_pass(const __grid_constant__ PassDesc d, const __grid_constant
     vec2_t* src = bufA;
     vec2_t* dst = bufB;
     for (int p = 0; p < d.nrad; ++p) {
-        run_inner<INV>(d.rad[p], src, dst, d.R, d.C, x.step[p], d.tw_inner);
+        run_inner<INV, BIG>(d.rad[p], src, dst, d.R, d.C, x.step[p], d.tw_inner);
         __syncthreads();
         vec2_t* t = src;
         src = dst;
@@ -466,16 +475,92 @@ __global__ void k_pass(const __grid_constant__ PassDesc d, const __grid_constant
     }
 }
 
+template <bool INV, bool BIG>
+__global__ void __launch_bounds__(kPassThreads) k_pass(const __grid_constant__ PassDesc d,
+                                                       const __grid_constant__ PassExtra x) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_body<INV, BIG>(d, x, blockIdx.x, reinterpret_cast<vec2_t*>(smem_raw));
+}
+
+// ---------------------------------------------------------------------------
+// persistent work-queue kernel: items (pass, tile) ordered by dependency level
+// ---------------------------------------------------------------------------
+struct QueueItem {
+    uint32_t desc;
+    uint32_t tile;
+};
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Waits for all tiles of pass `dep` to finish; a bounded spin that reports
+// failure instead of hanging.
+__device__ __forceinline__ bool wait_for(const uint32_t* done, uint32_t need) {
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
+        if (load_acquire(done) >= need) return true;
+        __nanosleep(200);
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kPassThreads) k_persistent(
+    const PassDesc* __restrict__ descs, const PassExtra* __restrict__ extras,
+    const int32_t* __restrict__ deps, const QueueItem* __restrict__ items, uint32_t nitems,
+    uint32_t* head, uint32_t* done, uint32_t* error) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_ok;
+    __shared__ __align__(16) PassDesc s_desc;
+    __shared__ __align__(16) PassExtra s_extra;
+    vec2_t* buf = reinterpret_cast<vec2_t*>(smem_raw);
+    while (true) {
+        if (threadIdx.x == 0) s_item = atomicAdd(head, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= nitems) return;
+        const QueueItem q = items[it];
+        if (threadIdx.x == 0) {
+            bool ok = true;
+            const int32_t dep = deps[q.desc];
+            if (dep >= 0) ok = wait_for(&done[dep], descs[dep].tiles);
+            if (!ok) atomicExch(error, 1u);
+            s_ok = ok ? 1u : 0u;
+        }
+        // stage the descriptor in shared memory
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&descs[q.desc]);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_desc);
+            for (uint32_t i = threadIdx.x; i < sizeof(PassDesc) / 4; i += blockDim.x) dst[i] = src[i];
+            const uint32_t* xs = reinterpret_cast<const uint32_t*>(&extras[q.desc]);
+            uint32_t* xd = reinterpret_cast<uint32_t*>(&s_extra);
+            for (uint32_t i = threadIdx.x; i < sizeof(PassExtra) / 4; i += blockDim.x) xd[i] = xs[i];
+        }
+        __syncthreads();
+        if (s_ok) {
+            if (s_desc.inv) tile_body<true, false>(s_desc, s_extra, q.tile, buf);
+            else tile_body<false, false>(s_desc, s_extra, q.tile, buf);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(&done[q.desc], 1u);
+    }
+}
+
 static bool configure_pass_kernels() {
     static bool done = false;
     if (done) return true;
-    cudaError_t e1 = cudaFuncSetAttribute(k_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          227 * 1024);
-    cudaError_t e2 = cudaFuncSetAttribute(k_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          227 * 1024);
-    if (e1 != cudaSuccess || e2 != cudaSuccess) {
-        note_cuda_error(e1 != cudaSuccess ? e1 : e2);
-        return false;
+    const void* fns[4] = {(const void*)k_pass<false, false>, (const void*)k_pass<true, false>,
+                          (const void*)k_pass<false, true>, (const void*)k_pass<true, true>};
+    for (const void* f : fns) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             227 * 1024);
+        if (e != cudaSuccess) {
+            note_cuda_error(e);
+            return false;
+        }
     }
     done = true;
     return true;
@@ -483,7 +568,23 @@ static bool configure_pass_kernels() {
 
 void launch_pass(const PassDesc& d, cudaStream_t st) {
     if (!configure_pass_kernels()) return;
+    const PassExtra x = make_extra(d);
+    bool big = false;
+    for (int p = 0; p < d.nrad; ++p) big = big || d.rad[p] > 16;
+    if (d.inv) {
+        if (big) k_pass<true, true><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
+        else k_pass<true, false><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
+    } else {
+        if (big) k_pass<false, true><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
+        else k_pass<false, false><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
+    }
+    note_cuda_error(cudaGetLastError());
+    count_launch();
+}
+
+PassExtra make_extra(const PassDesc& d) {
     PassExtra x;
+    memset(&x, 0, sizeof(x));
     uint32_t ns = 1;
     for (int p = 0; p < d.nrad; ++p) {
         const uint32_t P = d.rad[p];
@@ -495,12 +596,48 @@ void launch_pass(const PassDesc& d, cudaStream_t st) {
         s.div_ns.init(ns);
         ns *= P;
     }
-    if (d.inv)
-        k_pass<true><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
-    else
-        k_pass<false><<<d.tiles, d.threads, d.smem_bytes, st>>>(d, x);
+    return x;
+}
+
+size_t pass_extra_bytes() { return sizeof(PassExtra); }
+
+void fill_extras(const PassDesc* d, void* extras, size_t n) {
+    PassExtra* x = static_cast<PassExtra*>(extras);
+    for (size_t i = 0; i < n; ++i) x[i] = make_extra(d[i]);
+}
+
+bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
+                       const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
+                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st) {
+    static int blocks_per_sm = -1;
+    static uint32_t configured_smem = 0;
+    static int sms = 0;
+    if (configured_smem < smem_bytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem_bytes));
+        if (e != cudaSuccess) {
+            note_cuda_error(e);
+            return false;
+        }
+        configured_smem = smem_bytes;
+        blocks_per_sm = -1;
+    }
+    if (blocks_per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_persistent, kPassThreads,
+                                                      smem_bytes);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    uint32_t grid = uint32_t(sms * blocks_per_sm);
+    if (grid > nitems) grid = nitems ? nitems : 1;
+    k_persistent<<<grid, kPassThreads, smem_bytes, st>>>(
+        descs, static_cast<const PassExtra*>(extras), deps, static_cast<const QueueItem*>(items),
+        nitems, head, done, error);
     note_cuda_error(cudaGetLastError());
     count_launch();
+    return true;
 }
 
 // ---------------------------------------------------------------------------

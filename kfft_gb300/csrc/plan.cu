@@ -62,10 +62,10 @@ static std::vector<uint32_t> prime_factors(uint32_t n) {
     return f;
 }
 
-bool is_direct_length(uint32_t n) {
+bool is_direct_length(uint32_t n, uint32_t max_prime) {
     if (n == 0) return false;
     for (uint32_t p : prime_factors(n))
-        if (p > kMaxDirectPrime) return false;
+        if (p > max_prime) return false;
     return true;
 }
 
@@ -272,12 +272,13 @@ static bool transform_once(const FftPlan& plan, const vec2_t* in, vec2_t* out, c
     return ok;
 }
 
-FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st) {
+FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
+                   uint32_t max_prime) {
     FftPlan* P = new FftPlan();
     P->N = N;
     P->sign = sign;
     if (N == 0) return P;
-    if (is_direct_length(N)) {
+    if (is_direct_length(N, max_prime)) {
         P->method = METHOD_DIRECT;
         if (!build_direct(P, arena, st)) {
             delete P;
@@ -285,7 +286,7 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st) {
         }
         return P;
     }
-    if (is_prime(N) && is_direct_length(N - 1)) {
+    if (is_prime(N) && is_direct_length(N - 1, max_prime)) {
         // ---- Rader: X[g^-q] = x0 + sum_j x[g^j] W^(g^(j-q)) ------------------
         P->method = METHOD_RADER;
         const uint32_t L = N - 1;
@@ -313,8 +314,8 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st) {
         cudaMemcpyAsync(dip, ip.data(), sizeof(uint32_t) * L, cudaMemcpyHostToDevice, st);
         P->gperm = dgp;
         P->iperm = dip;
-        P->sub_fwd = make_plan(L, -1, arena, st);
-        P->sub_inv = make_plan(L, +1, arena, st);
+        P->sub_fwd = make_plan(L, -1, arena, st, max_prime);
+        P->sub_inv = make_plan(L, +1, arena, st, max_prime);
         if (!P->sub_fwd || !P->sub_inv) {
             delete P;
             return nullptr;
@@ -346,8 +347,8 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st) {
     }
     gen_chirp(chirp, N, N, sign, st);
     gen_bluestein_filter(filt, chirp, N, uint32_t(M), st);
-    P->sub_fwd = make_plan(uint32_t(M), -1, arena, st);
-    P->sub_inv = make_plan(uint32_t(M), +1, arena, st);
+    P->sub_fwd = make_plan(uint32_t(M), -1, arena, st, max_prime);
+    P->sub_inv = make_plan(uint32_t(M), +1, arena, st, max_prime);
     if (!P->sub_fwd || !P->sub_inv) {
         delete P;
         return nullptr;
@@ -454,7 +455,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     uint32_t elems = C * s.R;
     uint32_t t = (elems + 7) / 8;
     t = (t + 31) / 32 * 32;
-    d.threads = std::max<uint32_t>(64, std::min<uint32_t>(512, t));
+    d.threads = std::max<uint32_t>(64, std::min<uint32_t>(kPassThreads, t));
     d.smem_bytes = smem_for(elems);
     d.div_R.init(s.R);
     d.div_lanes_j.init(d.lanes_j);
@@ -548,7 +549,9 @@ bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t*
         ff.epi_op = EPI_MUL;
         ff.epi_tab = P.spectrum;
         Layout lx = lin;  // the input seen as length-L sequences with the caller's strides
+        const size_t mark = ws.used;
         if (!build_direct_passes(*P.sub_fwd, in, lx, A, la, real_t(1), ff, ws, descs)) return false;
+        ws.used = mark;  // the inverse reuses the forward's scratch (stream ordered)
         Fuse fi;
         fi.epi_op = EPI_CHIRP;
         fi.epi_tab = P.chirp;
@@ -566,7 +569,9 @@ bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t*
     ff.aux_in = in;
     ff.aux_in_bs = lin.bs;
     ff.aux_out = pairs;
+    const size_t mark = ws.used;
     if (!build_direct_passes(*P.sub_fwd, in, lin, A, la, real_t(1), ff, ws, descs)) return false;
+    ws.used = mark;  // the inverse reuses the forward's scratch (stream ordered)
     Fuse fi;
     fi.epi_op = EPI_RADER_INV;
     fi.epi_perm = P.iperm;
