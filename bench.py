@@ -178,10 +178,10 @@ class C2C4096(Workload):
 class Uneven(Workload):
     precision = "float"
 
-    def __init__(self, lib, precision="float"):
+    def __init__(self, lib, precision="float", subset=1):
         self.lib = lib
         self.precision = precision
-        self.lengths = uneven_lengths()
+        self.lengths = np.ascontiguousarray(uneven_lengths()[::subset])
         self.total = int(self.lengths.sum(dtype=np.int64))
         self.name = (f"uneven batch: {len(self.lengths)} complex {'fp32' if precision == 'float' else 'fp64'}"
                      f" sequences, lengths log-uniform in [16, 2^20], {self.total} points, forward")
@@ -224,25 +224,26 @@ class Uneven(Workload):
         return b, b
 
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
-        # bounded sample: every 16th sequence, timed until the budget is spent
+        # bounded sample: every 16th sequence of the batch, all host threads,
+        # OpenMP over sequences; repeated until the budget is spent
         idx = np.arange(0, len(self.lengths), 16)
         offs = np.concatenate([[0], np.cumsum(self.lengths.astype(np.int64))])
-        x = self.host_in.numpy().astype(np.complex128)
-        flops, t0, done = 0.0, time.perf_counter(), 0
-        plans = {}
-        while time.perf_counter() - t0 < budget_s:
-            for i in idx:
-                n = int(self.lengths[i])
-                p = plans.get(n) or plans.setdefault(n, oracle_mod.CpxPlan(n, 0))
-                p(x[offs[i]:offs[i] + n], threads)
-                flops += 5.0 * n * math.log2(max(n, 2))
-                if time.perf_counter() - t0 > budget_s:
-                    break
-            done += 1
-        el = time.perf_counter() - t0
-        for p in plans.values():
-            p.close()
-        return flops / el / 1e9, f"every 16th sequence ({len(idx)} of {len(self.lengths)}), {el:.1f}s"
+        x = np.asarray(self.host_in.numpy(), dtype=np.complex128)
+        sub_len = self.lengths[idx]
+        sub = np.concatenate([x[offs[i]:offs[i] + int(self.lengths[i])] for i in idx])
+        n = sub_len.astype(np.float64)
+        flops_call = float(np.sum(5.0 * n * np.log2(np.maximum(n, 2))))
+        plan = oracle_mod.UnevenPlan(sub_len, 0)  # planning is outside the timer
+        calls, t0 = 0, time.perf_counter()
+        while True:
+            plan(sub, threads)
+            calls += 1
+            el = time.perf_counter() - t0
+            if el > budget_s:
+                break
+        plan.close()
+        return flops_call * calls / el / 1e9, (f"every 16th sequence ({len(idx)} of {len(self.lengths)}, "
+                                               f"{int(n.sum())} points) x{calls}, {el:.1f}s")
 
 
 # ---------------------------------------------------------------------------
@@ -327,7 +328,8 @@ def run_reference(args, ws, rank):
 
     class _NoLib:
         L = None
-    wl = make_workload(args.workload, _NoLib(), need_lib=False)
+    wl = make_workload(args.workload, _NoLib(), need_lib=False, subset=args.subset,
+                       precision=args.precision)
     threads = os.cpu_count() or 1
     if isinstance(wl, Uneven):
         g = np.random.default_rng(2)
@@ -359,10 +361,10 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-def make_workload(name, lib, need_lib=True):
+def make_workload(name, lib, need_lib=True, subset=1, precision="float"):
     if name == "c2c4096":
         return C2C4096(lib)
-    return Uneven(lib)
+    return Uneven(lib, precision=precision, subset=subset)
 
 
 def main():
@@ -374,6 +376,10 @@ def main():
     ap.add_argument("--workload", default=os.environ.get("KFFT_BENCH_WORKLOAD", "uneven"),
                     choices=["uneven", "c2c4096"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--subset", type=int, default=1,
+                    help="profiling only: keep every k-th sequence of the uneven batch")
+    ap.add_argument("--precision", default="float", choices=["float", "double"],
+                    help="uneven workload precision")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -391,9 +397,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    probe = make_workload(args.workload, None)
+    probe = make_workload(args.workload, None, subset=args.subset, precision=args.precision)
     lib = kfft_gb300.load(probe.precision)
-    wl = make_workload(args.workload, lib)
+    wl = make_workload(args.workload, lib, subset=args.subset, precision=args.precision)
     nbuf = 1
     if hasattr(wl, "bytes_per_buffer"):
         nbuf = max(1, int(math.ceil(268e6 / wl.bytes_per_buffer())))

@@ -56,6 +56,13 @@ constexpr uint32_t kPadShift = 3;
 #endif
 __device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> kPadShift); }
 
+// global loads each thread keeps in flight in the tile load phase
+#if defined(KFFT_HALF_SCALAR)
+constexpr int kLoadUnroll = 8;
+#else
+constexpr int kLoadUnroll = 4;
+#endif
+
 // ---------------------------------------------------------------------------
 // compile-time trigonometry for the odd-prime butterflies: cos/sin(2 pi m / P)
 // from an exact octant reduction and Taylor series on [0, pi/4].
@@ -402,38 +409,56 @@ __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x,
     const uint32_t total_lanes = d.batch * d.lanes_j;
     const uint32_t lane0 = tile * d.C;
 
-    // ---- load -----------------------------------------------------------
-    for (uint32_t idx = threadIdx.x; idx < tile_elems; idx += blockDim.x) {
-        uint32_t c, r;
-        if (d.load_mode == MODE_LANE) {
-            r = fdiv(idx, d.div_C);
-            c = idx - r * d.C;
-        } else {
-            c = fdiv(idx, d.div_R);
-            r = idx - c * d.R;
-        }
-        const uint32_t g = lane0 + c;
-        vec2_t v = {real_t(0), real_t(0)};
-        if (g < total_lanes) {
-            uint32_t b, j;
-            if (d.order == ORDER_J) {
-                b = fdiv(g, d.div_lanes_j);
-                j = g - b * d.lanes_j;
+    // ---- load: kLoadUnroll independent loads per thread in flight ---------
+    for (uint32_t base = threadIdx.x; base < tile_elems; base += kLoadUnroll * blockDim.x) {
+        vec2_t v[kLoadUnroll];
+        uint32_t slot[kLoadUnroll];
+        uint32_t twe[kLoadUnroll];
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u) {
+            const uint32_t idx = base + u * blockDim.x;
+            v[u] = {real_t(0), real_t(0)};
+            slot[u] = 0xffffffffu;
+            twe[u] = 0;
+            if (idx >= tile_elems) continue;
+            uint32_t c, r;
+            if (d.load_mode == MODE_LANE) {
+                r = fdiv(idx, d.div_C);
+                c = idx - r * d.C;
             } else {
-                j = fdiv(g, d.div_batch);
-                b = g - j * d.batch;
+                c = fdiv(idx, d.div_R);
+                r = idx - c * d.R;
             }
-            v = load_elem(d, b, j + r * d.lanes_j);
-            if (d.Ns > 1) {
-                const uint32_t kq = fdiv(j, d.div_Ns);
-                const uint32_t k = j - kq * d.Ns;
-                const uint64_t e = uint64_t(r) * k * d.tw_mul;
-                const uint32_t lo = uint32_t(e & ((uint64_t(1) << d.tw_shift) - 1));
-                const uint32_t hi = uint32_t(e >> d.tw_shift);
-                v = cmul(v, cmul(__ldg(&d.tw_hi[hi]), __ldg(&d.tw_lo[lo])));
+            slot[u] = pad(c * d.R + r);
+            const uint32_t g = lane0 + c;
+            if (g < total_lanes) {
+                uint32_t b, j;
+                if (d.order == ORDER_J) {
+                    b = fdiv(g, d.div_lanes_j);
+                    j = g - b * d.lanes_j;
+                } else {
+                    j = fdiv(g, d.div_batch);
+                    b = g - j * d.batch;
+                }
+                v[u] = load_elem(d, b, j + r * d.lanes_j);
+                if (d.Ns > 1) {
+                    const uint32_t kq = fdiv(j, d.div_Ns);
+                    const uint32_t k = j - kq * d.Ns;
+                    twe[u] = uint32_t(uint64_t(r) * k * d.tw_mul);
+                }
             }
         }
-        bufA[pad(c * d.R + r)] = v;
+        if (d.Ns > 1) {
+            const uint32_t mask = (1u << d.tw_shift) - 1u;
+#pragma unroll
+            for (int u = 0; u < kLoadUnroll; ++u) {
+                const vec2_t w = cmul(__ldg(&d.tw_hi[twe[u] >> d.tw_shift]), __ldg(&d.tw_lo[twe[u] & mask]));
+                v[u] = cmul(v[u], w);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u)
+            if (slot[u] != 0xffffffffu) bufA[slot[u]] = v[u];
     }
     __syncthreads();
 

@@ -437,6 +437,80 @@ int oracle_exec_cpx_batch(const void* plan, const ocpx* in, ocpx* out, uint64_t 
     return ret;
 }
 
+/* Uneven batch: sequences of lengths[i] packed back to back, one plan per
+ * distinct length built once, OpenMP over sequences at execution (the
+ * host-loop pattern of ext/2d/kfft_cpx2.c:100-104 applied to a list of
+ * lengths). */
+typedef struct {
+    uint32_t count;
+    uint64_t* off;
+    oplan** plans; /* per sequence; equal lengths share one plan */
+    uint8_t* owner;
+} ouneven;
+
+void* oracle_uneven_create(uint32_t count, const uint32_t* lengths, uint32_t flags) {
+    ouneven* U = (ouneven*)calloc(1, sizeof(ouneven));
+    if (!U) return NULL;
+    U->count = count;
+    U->off = (uint64_t*)malloc(sizeof(uint64_t) * (count + 1));
+    U->plans = (oplan**)calloc(count ? count : 1, sizeof(oplan*));
+    U->owner = (uint8_t*)calloc(count ? count : 1, 1);
+    if (!U->off || !U->plans || !U->owner) {
+        oracle_uneven_free(U);
+        return NULL;
+    }
+    U->off[0] = 0;
+    for (uint32_t i = 0; i < count; i++) U->off[i + 1] = U->off[i] + lengths[i];
+    for (uint32_t i = 0; i < count; i++) {
+        for (uint32_t j = 0; j < i; j++)
+            if (lengths[j] == lengths[i]) {
+                U->plans[i] = U->plans[j];
+                break;
+            }
+        if (!U->plans[i]) {
+            U->plans[i] = (oplan*)oracle_plan_cpx(lengths[i], flags);
+            U->owner[i] = 1;
+            if (!U->plans[i]) {
+                oracle_uneven_free(U);
+                return NULL;
+            }
+        }
+    }
+    return U;
+}
+
+int oracle_uneven_exec(const void* u, const ocpx* in, ocpx* out, int threads) {
+    const ouneven* U = (const ouneven*)u;
+    int ret = OR_RET_SUCCESS;
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt) reduction(| : ret)
+    for (int64_t i = 0; i < (int64_t)U->count; i++)
+        ret |= plan_exec(U->plans[i], in + U->off[i], out + U->off[i]);
+    return ret;
+}
+
+void oracle_uneven_free(void* u) {
+    ouneven* U = (ouneven*)u;
+    if (!U) return;
+    if (U->plans && U->owner)
+        for (uint32_t i = 0; i < U->count; i++)
+            if (U->owner[i]) plan_destroy(U->plans[i]);
+    free(U->plans);
+    free(U->owner);
+    free(U->off);
+    free(U);
+}
+
+int oracle_exec_uneven(uint32_t count, const uint32_t* lengths, uint32_t flags, const ocpx* in,
+                       ocpx* out, int threads) {
+    void* U = oracle_uneven_create(count, lengths, flags);
+    if (!U) return OR_RET_ALLOC_FAIL;
+    int r = oracle_uneven_exec(U, in, out, threads);
+    oracle_uneven_free(U);
+    return r;
+}
+
 int oracle_fft_cpx(uint32_t nfft, uint32_t flags, const ocpx* in, ocpx* out) {
     oplan* P = (oplan*)oracle_plan_cpx(nfft, flags);
     if (!P) return OR_RET_ALLOC_FAIL;

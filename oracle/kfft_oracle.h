@@ -39,6 +39,11 @@ int oracle_exec_cpx(const void* plan, const ocpx* in, ocpx* out);
 int oracle_exec_cpx_batch(const void* plan, const ocpx* in, ocpx* out, uint64_t batch,
                           int threads);
 int oracle_fft_cpx(uint32_t nfft, uint32_t flags, const ocpx* in, ocpx* out);
+void* oracle_uneven_create(uint32_t count, const uint32_t* lengths, uint32_t flags);
+int oracle_uneven_exec(const void* u, const ocpx* in, ocpx* out, int threads);
+void oracle_uneven_free(void* u);
+int oracle_exec_uneven(uint32_t count, const uint32_t* lengths, uint32_t flags, const ocpx* in,
+                       ocpx* out, int threads);
 int oracle_rfft(uint32_t nfft, uint32_t flags, const double* in, ocpx* out);
 int oracle_irfft(uint32_t nfft, uint32_t flags, const ocpx* in, double* out);
 int oracle_fft2_cpx(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, ocpx* out);

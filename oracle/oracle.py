@@ -74,6 +74,11 @@ def _load():
         lib.oracle_conv2_cpx.argtypes = [u32, u32, u32, vp, vp, vp]
         lib.oracle_conv2_scalar.argtypes = [u32, u32, u32, vp, vp, vp]
         lib.oracle_dft_exact.argtypes = [u32, i32, vp, vp]
+        lib.oracle_exec_uneven.argtypes = [u32, vp, u32, vp, vp, i32]
+        lib.oracle_uneven_create.restype = vp
+        lib.oracle_uneven_create.argtypes = [u32, vp, u32]
+        lib.oracle_uneven_exec.argtypes = [vp, vp, vp, i32]
+        lib.oracle_uneven_free.argtypes = [vp]
         _lib = lib
         return lib
 
@@ -220,6 +225,51 @@ def conv2_scalar(a, b, flags: int = 0):
     _check(lib.oracle_conv2_scalar(x, y, flags, a.ctypes.data, b.ctypes.data,
                                    out.ctypes.data), "conv2_scalar")
     return out
+
+
+def fft_uneven(lengths, x, flags: int = 0, threads: int = 0):
+    """Transforms sequences of the given lengths packed back to back."""
+    lib = _load()
+    lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
+    x = _c128(x)
+    if x.size != int(lengths.sum(dtype=np.int64)):
+        raise ValueError("input size does not match the lengths")
+    y = np.empty_like(x)
+    _check(lib.oracle_exec_uneven(lengths.size, lengths.ctypes.data, flags, x.ctypes.data,
+                                  y.ctypes.data, threads), "exec_uneven")
+    return y
+
+
+class UnevenPlan:
+    """Oracle plans for a packed batch of uneven lengths, built once."""
+
+    def __init__(self, lengths, flags: int = 0):
+        self.lib = _load()
+        self.lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
+        self.total = int(self.lengths.sum(dtype=np.int64))
+        self.ptr = self.lib.oracle_uneven_create(self.lengths.size, self.lengths.ctypes.data, flags)
+        if not self.ptr:
+            raise MemoryError("oracle uneven plan failed")
+
+    def __call__(self, x, threads: int = 0):
+        x = _c128(x)
+        if x.size != self.total:
+            raise ValueError("input size does not match the lengths")
+        y = np.empty_like(x)
+        _check(self.lib.oracle_uneven_exec(self.ptr, x.ctypes.data, y.ctypes.data, threads),
+               "uneven_exec")
+        return y
+
+    def close(self):
+        if self.ptr:
+            self.lib.oracle_uneven_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def dft_exact(x, inverse: bool = False):

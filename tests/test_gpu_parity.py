@@ -249,3 +249,30 @@ def test_release_frees_device_memory(lib):
     assert lib.stats().device_bytes > before
     assert lib.cleanup(p) == 0
     assert lib.stats().device_bytes == before
+
+
+@pytest.mark.parametrize("precision", ["double", "float"])
+def test_uneven_workload_subset(precision):
+    """Every 8th sequence of the uneven-batch benchmark workload, both builds."""
+    import bench
+    lib = K.load(precision)
+    lengths = np.ascontiguousarray(bench.uneven_lengths()[::8])
+    total = int(lengths.sum(dtype=np.int64))
+    rng = np.random.default_rng(2)
+    x = cx(rng, total)
+    cdt = np.complex128 if precision == "double" else np.complex64
+    xin = x.astype(cdt)
+    p = lib.L.kfft_config_cpx_uneven(len(lengths), lengths.ctypes.data, 0)
+    assert p, lib.last_error()
+    y = np.empty_like(xin)
+    assert lib.L.kfft_eval_cpx_uneven(p, xin.ctypes.data, y.ctypes.data) == 0
+    lib.L.kfft_release_uneven(p)
+    ref = O.fft_uneven(lengths, xin.astype(np.complex128))
+    off = 0
+    worst = 0.0
+    for n in lengths:
+        n = int(n)
+        e = rel_l2(y[off:off + n], ref[off:off + n])
+        worst = max(worst, e / (tol64(n) if precision == "double" else TOL32))
+        off += n
+    assert worst <= 1.0, worst
