@@ -59,6 +59,27 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven_async(kfft_plan_uneven* plan, const 
 KFFT_API uint64_t kfft_uneven_total(const kfft_plan_uneven* plan);
 KFFT_API void kfft_release_uneven(kfft_plan_uneven* plan);
 
+/*
+ * Complex transform that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc (code inside a CUDA graph
+ * capture or another library's stream-ordered region, real-time loops that
+ * forbid allocator calls and the synchronisation cudaFree implies, or a host
+ * whose framework must own every allocation).  fin/fout are device buffers of
+ * `batch` back-to-back sequences; the work is queued on `stream` (a
+ * cudaStream_t) and the call returns without waiting.  The plan must be a
+ * direct mixed-radix plan (every prime factor of nfft <= 31).  Scratch between
+ * passes lives in one file-scope device array of kfft_noalloc_scratch_bytes()
+ * bytes (32 MiB) that every GPU loading this library holds until the process
+ * exits; requests that need more return KFFT_RET_BADARGUMENTS and
+ * kfft_noalloc_last_message() says why.  The first call on each device looks
+ * up the array's device address and should be made before any stream capture.
+ * All calls share the array: calls whose kernels overlap on the GPU race.
+ */
+KFFT_API kfft_return_t kfft_eval_cpx_noalloc(kfft_plan_cpx* plan, const kfft_cpx* fin,
+                                             kfft_cpx* fout, uint32_t batch, void* stream);
+KFFT_API size_t kfft_noalloc_scratch_bytes(void);
+KFFT_API const char* kfft_noalloc_last_message(void);
+
 /* Engine introspection (used by tests and the benchmark). */
 typedef struct {
     uint64_t kernel_launches; /* kernels this library launched since load */

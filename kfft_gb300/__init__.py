@@ -51,6 +51,7 @@ EXPORTED_SYMBOLS = [
     "kfft_config_cpx_uneven", "kfft_eval_cpx_uneven", "kfft_eval_cpx_uneven_async",
     "kfft_uneven_total", "kfft_release_uneven",
     "kfft_gb300_stats", "kfft_gb300_last_error", "kfft_gb300_describe",
+    "kfft_eval_cpx_noalloc", "kfft_noalloc_scratch_bytes", "kfft_noalloc_last_message",
 ]
 
 
@@ -145,6 +146,10 @@ class KfftLib:
         L.kfft_free_null.argtypes = [ctypes.POINTER(vp)]
         L.kfft_info.argtypes = [ctypes.POINTER(InfoT)]
         L.kfft_gb300_stats.argtypes = [ctypes.POINTER(Stats)]
+        L.kfft_eval_cpx_noalloc.restype = ctypes.c_uint
+        L.kfft_eval_cpx_noalloc.argtypes = [vp, vp, vp, u32, vp]
+        L.kfft_noalloc_scratch_bytes.restype = sz
+        L.kfft_noalloc_last_message.restype = ctypes.c_char_p
         L.kfft_gb300_last_error.restype = ctypes.c_char_p
         L.kfft_gb300_describe.restype = ctypes.c_char_p
         L.kfft_gb300_describe.argtypes = [vp]

@@ -22,7 +22,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
-SOURCES = ["kernels.cu", "plan.cu", "api.cu", "uneven.cu"]
+SOURCES = ["kernels.cu", "plan.cu", "api.cu", "uneven.cu", "noalloc.cu"]
 HEADERS = ["engine.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libkfft_gb300.so": [], "libkfft_gb300_f.so": ["-DKFFT_HALF_SCALAR"]}

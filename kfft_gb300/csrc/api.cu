@@ -126,6 +126,12 @@ struct kfft_gpu_plan {
     }
 };
 
+namespace kfft {
+const FftPlan* device_plan_of(const kfft_plan_cpx* p) {
+    return (p && p->gpu) ? p->gpu->plan : nullptr;
+}
+}  // namespace kfft
+
 namespace {
 struct PoolRegistry {
     std::vector<kfft_gpu_plan*> plans;

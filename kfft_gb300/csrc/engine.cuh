@@ -218,6 +218,12 @@ size_t workspace_bytes(const FftPlan& p, uint32_t batch);
 bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t* out,
                   const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
+// Descriptor of pass `pass` of a DIRECT plan (no fused element operations).
+PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const Layout& lin,
+                        vec2_t* out, const Layout& lout, real_t scale);
+
+// The device plan behind a public complex plan handle (nullptr if none).
+const FftPlan* device_plan_of(const kfft_plan_cpx* p);
 
 // ---- runtime ----------------------------------------------------------------
 int current_device();

@@ -471,6 +471,11 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     return d;
 }
 
+PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const Layout& lin,
+                        vec2_t* out, const Layout& lout, real_t scale) {
+    return make_desc(P, pass, in, lin, out, lout, scale);
+}
+
 static void apply_fuse(PassDesc& d, const Fuse& f, bool first, bool last) {
     if (first) {
         d.pro_op = f.pro_op;
