@@ -100,17 +100,30 @@ class Workload:
         raise NotImplementedError
 
 
-class C2C4096(Workload):
-    name = "c2c fp64 N=4096 batch 256 forward+inverse"
-    precision = "double"
-    N, B = 4096, 256
+class Uniform(Workload):
+    """B complex sequences of one length N, forward then inverse per step."""
 
-    def __init__(self, lib):
+    def __init__(self, lib, N, B, precision, seed, dist_name):
         self.lib = lib
+        self.N, self.B, self.precision, self.seed = N, B, precision, seed
+        self.dist_name = dist_name
+        tag = "fp64" if precision == "double" else "fp32"
+        self.name = f"c2c {tag} N={N} batch {B} forward+inverse"
+
+    def _cdt(self):
+        return np.complex128 if self.precision == "double" else np.complex64
+
+    def _input(self):
+        rng = np.random.default_rng(self.seed)
+        shape = (self.B, self.N)
+        if self.dist_name == "uniform":
+            x = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        else:
+            x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        return x.astype(self._cdt())
 
     def setup(self, torch, dev, nbuf):
-        rng = np.random.default_rng(1)
-        x = rng.uniform(-1, 1, (self.B, self.N)) + 1j * rng.uniform(-1, 1, (self.B, self.N))
+        x = self._input()
         self.host_in = x
         self.fwd = self.lib.L.kfft_config_cpx(self.N, 0, None, None)
         self.inv = self.lib.L.kfft_config_cpx(self.N, 1, None, None)
@@ -123,17 +136,23 @@ class C2C4096(Workload):
         self.pin_mid = torch.empty_like(self.pin_in).pin_memory()
         self.pin_out = torch.empty_like(self.pin_in).pin_memory()
 
+    def elem_bytes(self):
+        return 16 if self.precision == "double" else 8
+
     def bytes_per_buffer(self):
-        return self.N * self.B * 16
+        return self.N * self.B * self.elem_bytes()
 
     def flops_per_step(self):
-        return 2 * 5.0 * self.N * math.log2(self.N) * self.B
+        return 2 * 5.0 * self.N * math.log2(max(self.N, 2)) * self.B
 
     def launches_per_step(self):
-        return 2
+        return None  # one or more passes per transform; see roofline()
 
     def algorithmic_bytes_per_launch(self):
-        return 2 * self.N * self.B * 16  # read once, write once
+        return None
+
+    def algorithmic_bytes_per_step(self):
+        return 2 * 2 * self.N * self.B * self.elem_bytes()  # fwd + inv, read + write once
 
     def step(self, i, stream):
         L = self.lib.L
@@ -150,13 +169,13 @@ class C2C4096(Workload):
         assert r1 == 0 and r2 == 0
 
     def e2e_bytes(self):
-        b = self.N * self.B * 16
+        b = self.bytes_per_buffer()
         return 2 * b, 2 * b
 
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
         fwd = oracle_mod.CpxPlan(self.N, 0)
         inv = oracle_mod.CpxPlan(self.N, 1)
-        x = self.host_in
+        x = self.host_in.astype(np.complex128)
         n_done, t0 = 0, time.perf_counter()
         while True:
             y = fwd(x, threads)
@@ -169,10 +188,18 @@ class C2C4096(Workload):
         inv.close()
         return self.flops_per_step() * n_done / el / 1e9, f"{n_done} steps of the full workload"
 
-    def check(self):
-        from oracle import oracle
-        y = self.out.cpu().numpy()
-        return float(np.linalg.norm(y - self.host_in) / np.linalg.norm(self.host_in))
+
+def C2C4096(lib):
+    return Uniform(lib, 4096, 256, "double", 1, "uniform")
+
+
+UNIFORM_WORKLOADS = {
+    "c2c4096": lambda lib: Uniform(lib, 4096, 256, "double", 1, "uniform"),
+    "c2c_f32_2p18x64": lambda lib: Uniform(lib, 1 << 18, 64, "float", 3, "normal"),
+    "c2c_f32_2p24": lambda lib: Uniform(lib, 1 << 24, 1, "float", 3, "normal"),
+    "c2c_f64_2p18x64": lambda lib: Uniform(lib, 1 << 18, 64, "double", 3, "normal"),
+    "c2c_f32_4096x4096": lambda lib: Uniform(lib, 4096, 4096, "float", 1, "uniform"),
+}
 
 
 class Uneven(Workload):
@@ -337,8 +364,7 @@ def run_reference(args, ws, rank):
         import types
         wl.host_in = types.SimpleNamespace(numpy=lambda: x)
     else:
-        rng = np.random.default_rng(1)
-        wl.host_in = rng.uniform(-1, 1, (wl.B, wl.N)) + 1j * rng.uniform(-1, 1, (wl.B, wl.N))
+        wl.host_in = wl._input()
     budget = max(2.0, 20.0 / max(args.steps + args.warmup, 1))
     vals, samples = [], []
     for _ in range(args.warmup):
@@ -362,8 +388,8 @@ def run_reference(args, ws, rank):
 
 
 def make_workload(name, lib, need_lib=True, subset=1, precision="float"):
-    if name == "c2c4096":
-        return C2C4096(lib)
+    if name in UNIFORM_WORKLOADS:
+        return UNIFORM_WORKLOADS[name](lib)
     return Uneven(lib, precision=precision, subset=subset)
 
 
@@ -374,7 +400,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("KFFT_BENCH_WORKLOAD", "uneven"),
-                    choices=["uneven", "c2c4096"])
+                    choices=["uneven"] + sorted(UNIFORM_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--subset", type=int, default=1,
                     help="profiling only: keep every k-th sequence of the uneven batch")
@@ -428,12 +454,7 @@ def main():
         pg.barrier()
     launches = lib.stats().kernel_launches - l0
     ms_total = start.elapsed_time(end)
-    if pg:
-        t = torch.tensor([ms_total], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms = ms_total / args.steps
-    value = ws * wl.flops_per_step() / (ms / 1e3) / 1e9
+    ms, value = aggregate_over_ranks(ms_total, wl.flops_per_step(), args.steps, ws, pg, dev)
 
     # end to end through the C ABI with pinned host buffers
     for _ in range(2):
@@ -471,9 +492,26 @@ def main():
         pg.destroy_process_group()
 
 
+def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, device="cpu"):
+    """Max step time over ranks and the whole-job throughput (weak scaling:
+    every rank runs the full per-GPU workload, replicas only)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms_total)], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms = ms_total / steps
+    return ms, world * flops_per_step / (ms / 1e3) / 1e9
+
+
 def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind):
     per = wl.algorithmic_bytes_per_launch()
     n = wl.launches_per_step()
+    if hasattr(wl, "algorithmic_bytes_per_step"):
+        achieved = wl.algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "kernel": "k_pass_reg / k_pass (all passes of the step)"}
     if per is None or not n:
         total_bytes = wl.total * (8 if wl.precision == "float" else 16) * 2
         achieved = total_bytes / (ms_step / 1e3) / 1e9

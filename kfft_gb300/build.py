@@ -22,8 +22,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
-SOURCES = ["kernels.cu", "plan.cu", "api.cu", "uneven.cu", "noalloc.cu"]
-HEADERS = ["engine.cuh"]
+SOURCES = ["pass_smem.cu", "pass_reg.cu", "persistent.cu", "tables.cu", "plan.cu", "api.cu",
+           "uneven.cu", "noalloc.cu"]
+HEADERS = ["engine.cuh", "fft_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libkfft_gb300.so": [], "libkfft_gb300_f.so": ["-DKFFT_HALF_SCALAR"]}
 
@@ -71,7 +72,7 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
             jobs.append((os.path.join(CSRC, s), obj, defines))
         jobs.append(("LINK", target, objs))
     compile_jobs = [j for j in jobs if j[0] != "LINK"]
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         list(ex.map(lambda j: _compile(*j), compile_jobs))
     for j in jobs:
         if j[0] == "LINK":

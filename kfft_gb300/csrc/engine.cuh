@@ -35,6 +35,10 @@ typedef double2 vec2_t;
 constexpr int kMaxInnerRadices = 12;
 // CTA size ceiling of the pass kernels (their register budget is sized for it).
 constexpr uint32_t kPassThreads = 256;
+// Largest tile (lanes x length) of the fused-I/O kernel (radices <= 16):
+// the first inner pass reads global memory, the last writes it, and the
+// passes between exchange through two shared-memory buffers.
+constexpr uint32_t kRegTile = 4096;
 // Largest prime factor a DIRECT plan accepts; larger primes go to Rader/Bluestein.
 constexpr uint32_t kMaxDirectPrime = 31;
 
@@ -80,6 +84,7 @@ struct PassDesc {
     uint32_t smem_bytes;     // dynamic shared memory
     uint8_t load_mode, store_mode, order;
     uint8_t inv;             // butterfly direction (tables already carry it)
+    uint8_t regmode;         // fused-I/O tile (radices <= 16, C*R <= kRegTile)
     uint8_t nrad;
     uint8_t rad[kMaxInnerRadices];
     FastDiv div_R, div_lanes_j, div_batch, div_Ns, div_C;
@@ -124,7 +129,8 @@ void launch_pass(const PassDesc& d, cudaStream_t st);
 // Persistent work-queue execution of many pass chains in one launch: `items`
 // lists (desc, tile) pairs ordered by dependency level; deps[d] is the pass
 // that must finish before any tile of pass d starts (-1: none).  A bounded wait
-// that gives up sets *error instead of hanging.  Radices must be <= 16.
+// that gives up sets *error instead of hanging.  Every pass must be a
+// register-resident tile (PassDesc::regmode).
 size_t pass_extra_bytes();
 void fill_extras(const PassDesc* d, void* extras, size_t n);
 bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,

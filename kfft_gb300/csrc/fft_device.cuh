@@ -1,0 +1,724 @@
+// fft_device.cuh -- device building blocks of the GB300 FFT engine: complex
+// helpers, register butterflies (radix 2/4/8/16 and odd primes 3..31), the
+// shared-memory Stockham tile (tile_body) and the register-resident tile
+// (tile_body_reg), and the element prologue/epilogue of fused Rader and
+// Bluestein passes.  Included by the kernel translation units.
+//
+// The tiles replace the reference's recursive kf_work (kfft_work.c:1-59) and
+// its butterflies kf_bfly2/3/4/5 and std_method_eval (kfft_bfly.c:1-152,
+// kfft_generic.c:9-36); the prologue/epilogue wiring replaces
+// rader_method_eval/kfft_part_convolution (kfft_rader.c).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+
+#include "engine.cuh"
+
+namespace kfft {
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return uint32_t((uint64_t(__umulhi(n, f.m)) + n) >> f.s);
+}
+
+__device__ __forceinline__ vec2_t cadd(vec2_t a, vec2_t b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ vec2_t csub(vec2_t a, vec2_t b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ vec2_t cmul(vec2_t a, vec2_t b) {
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__device__ __forceinline__ vec2_t cscale(vec2_t a, real_t s) { return {a.x * s, a.y * s}; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ vec2_t rot(vec2_t a) {
+    return INV ? vec2_t{-a.y, a.x} : vec2_t{a.y, -a.x};
+}
+
+// one padding slot per 128 bytes of shared memory
+#if defined(KFFT_HALF_SCALAR)
+constexpr uint32_t kPadShift = 4;
+#else
+constexpr uint32_t kPadShift = 3;
+#endif
+__device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> kPadShift); }
+
+// resident CTAs per SM the fused-I/O kernels are compiled for (register cap
+// 65536 / (256 * blocks)): three for FP32, two for FP64 (more would spill)
+#ifndef KFFT_REG_MINBLOCKS
+#if defined(KFFT_HALF_SCALAR)
+#define KFFT_REG_MINBLOCKS 3
+#else
+#define KFFT_REG_MINBLOCKS 2
+#endif
+#endif
+
+// global loads each thread keeps in flight in the tile load phase
+#if defined(KFFT_HALF_SCALAR)
+constexpr int kLoadUnroll = 8;
+#else
+constexpr int kLoadUnroll = 4;
+#endif
+
+// ---------------------------------------------------------------------------
+// compile-time trigonometry for the odd-prime butterflies: cos/sin(2 pi m / P)
+// from an exact octant reduction and Taylor series on [0, pi/4].
+// ---------------------------------------------------------------------------
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+constexpr double taylor_sin(double x) {
+    double x2 = x * x, term = x, sum = x;
+    for (int k = 1; k < 14; ++k) {
+        term *= -x2 / double((2 * k) * (2 * k + 1));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double taylor_cos(double x) {
+    double x2 = x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 14; ++k) {
+        term *= -x2 / double((2 * k - 1) * (2 * k));
+        sum += term;
+    }
+    return sum;
+}
+// returns cos (want_sin=false) or sin of 2*pi*m/P
+constexpr double trig_ratio(long m, long P, bool want_sin) {
+    m %= P;
+    if (m < 0) m += P;
+    long t = (8 * m) / P;          // octant 0..7
+    long r = 8 * m - t * P;        // remainder: angle = (t + r/P) * pi/4
+    double a = kPi / 4.0 * double(r) / double(P);
+    // for odd octants use the complement to keep the argument in [0, pi/4]
+    double s0 = 0, c0 = 0;
+    if (t & 1) {
+        double b = kPi / 4.0 * double(P - r) / double(P);
+        s0 = taylor_sin(b);
+        c0 = taylor_cos(b);
+        // angle = (t+1)*pi/4 - b
+        long q = (t + 1) / 2;  // multiples of pi/2
+        double sv = 0, cv = 0;
+        // sin(q*pi/2 - b), cos(q*pi/2 - b)
+        switch (q & 3) {
+            case 0: sv = -s0; cv = c0; break;
+            case 1: sv = c0; cv = s0; break;
+            case 2: sv = s0; cv = -c0; break;
+            default: sv = -c0; cv = -s0; break;
+        }
+        return want_sin ? sv : cv;
+    } else {
+        s0 = taylor_sin(a);
+        c0 = taylor_cos(a);
+        long q = t / 2;
+        double sv = 0, cv = 0;
+        // sin(q*pi/2 + a), cos(q*pi/2 + a)
+        switch (q & 3) {
+            case 0: sv = s0; cv = c0; break;
+            case 1: sv = c0; cv = -s0; break;
+            case 2: sv = -s0; cv = -c0; break;
+            default: sv = -c0; cv = s0; break;
+        }
+        return want_sin ? sv : cv;
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// butterflies (in registers)
+// ---------------------------------------------------------------------------
+template <bool INV>
+__device__ __forceinline__ void dft2(vec2_t& a, vec2_t& b) {
+    vec2_t t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(vec2_t& a0, vec2_t& a1, vec2_t& a2, vec2_t& a3) {
+    vec2_t s0 = cadd(a0, a2), s1 = csub(a0, a2);
+    vec2_t s2 = cadd(a1, a3), s3 = rot<INV>(csub(a1, a3));
+    a0 = cadd(s0, s2);
+    a2 = csub(s0, s2);
+    a1 = cadd(s1, s3);
+    a3 = csub(s1, s3);
+}
+
+constexpr double kR2 = 0.70710678118654752440084436210484903928;
+constexpr double kC8 = 0.92387953251128675612818318939678828682;  // cos(pi/8)
+constexpr double kS8 = 0.38268343236508977172845998403039886676;  // sin(pi/8)
+
+// multiply by W_8^k (forward W = exp(-2 pi i/8))
+template <bool INV, int K>
+__device__ __forceinline__ vec2_t w8(vec2_t a) {
+    const real_t r = real_t(kR2);
+    if constexpr (K == 0) return a;
+    else if constexpr (K == 2) return rot<INV>(a);
+    else if constexpr (K == 1) {
+        // (1 -+ i)/sqrt2 * a
+        return INV ? vec2_t{(a.x - a.y) * r, (a.x + a.y) * r}
+                   : vec2_t{(a.x + a.y) * r, (a.y - a.x) * r};
+    } else {  // K == 3: (-1 -+ i)/sqrt2
+        return INV ? vec2_t{-(a.x + a.y) * r, (a.x - a.y) * r}
+                   : vec2_t{(a.y - a.x) * r, -(a.x + a.y) * r};
+    }
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(vec2_t* v) {
+    // radix-2 first (stride 4), twiddle, then two radix-4
+    for (int i = 0; i < 4; ++i) dft2<INV>(v[i], v[i + 4]);
+    v[5] = w8<INV, 1>(v[5]);
+    v[6] = w8<INV, 2>(v[6]);
+    v[7] = w8<INV, 3>(v[7]);
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+    dft4<INV>(v[4], v[5], v[6], v[7]);
+    // outputs: v[i] -> X[2i], v[4+i] -> X[2i+1]
+    vec2_t t[8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        t[2 * i] = v[i];
+        t[2 * i + 1] = v[4 + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = t[i];
+}
+
+// multiply by W_16^k, k in 0..9
+template <bool INV>
+__device__ __forceinline__ vec2_t w16(vec2_t a, int k) {
+    const real_t c8 = real_t(kC8), s8 = real_t(kS8), r = real_t(kR2);
+    real_t wr, wi;
+    switch (k) {
+        case 1: wr = c8; wi = -s8; break;
+        case 2: wr = r; wi = -r; break;
+        case 3: wr = s8; wi = -c8; break;
+        case 4: return rot<INV>(a);
+        case 6: wr = -r; wi = -r; break;
+        case 9: wr = -c8; wi = s8; break;
+        default: return a;
+    }
+    if (INV) wi = -wi;
+    return {a.x * wr - a.y * wi, a.x * wi + a.y * wr};
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft16(vec2_t* v) {
+    // 4 radix-4 over stride 4, twiddle W16^(n1*k2), 4 radix-4, transpose
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dft4<INV>(v[i], v[i + 4], v[i + 8], v[i + 12]);
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+#pragma unroll
+        for (int k = 1; k < 4; ++k) v[i + 4 * k] = w16<INV>(v[i + 4 * k], i * k);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dft4<INV>(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    vec2_t t[16];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) t[k + 4 * i] = v[4 * k + i];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = t[i];
+}
+
+// odd prime P: symmetric-pair DFT, (P-1)^2 real multiply-adds.  The cosines
+// and sines are template-level constant expressions, so they become
+// instruction immediates rather than a table in memory.
+template <int P, int K, int N, int H>
+struct OddAcc {
+    __device__ static __forceinline__ void run(const vec2_t* s, const vec2_t* d, vec2_t& a,
+                                               vec2_t& b) {
+        constexpr real_t cc = real_t(trig_ratio(long(N) * K, P, false));
+        constexpr real_t ss = real_t(trig_ratio(long(N) * K, P, true));
+        a.x += s[N - 1].x * cc;
+        a.y += s[N - 1].y * cc;
+        b.x += d[N - 1].x * ss;
+        b.y += d[N - 1].y * ss;
+        if constexpr (N < H) OddAcc<P, K, N + 1, H>::run(s, d, a, b);
+    }
+};
+
+template <int P, bool INV, int K, int H>
+struct OddOut {
+    __device__ static __forceinline__ void run(vec2_t x0, const vec2_t* s, const vec2_t* d,
+                                               vec2_t* v) {
+        vec2_t a = x0, b = {real_t(0), real_t(0)};
+        OddAcc<P, K, 1, H>::run(s, d, a, b);
+        // forward: X_k = a - i b, X_{P-k} = a + i b; inverse swaps
+        const vec2_t ib = {-b.y, b.x};
+        if (INV) {
+            v[K] = cadd(a, ib);
+            v[P - K] = csub(a, ib);
+        } else {
+            v[K] = csub(a, ib);
+            v[P - K] = cadd(a, ib);
+        }
+        if constexpr (K < H) OddOut<P, INV, K + 1, H>::run(x0, s, d, v);
+    }
+};
+
+template <int P, bool INV>
+__device__ __forceinline__ void dft_odd(vec2_t* v) {
+    constexpr int H = (P - 1) / 2;
+    vec2_t s[H], d[H];
+    const vec2_t x0 = v[0];
+    vec2_t sum = v[0];
+#pragma unroll
+    for (int n = 1; n <= H; ++n) {
+        s[n - 1] = cadd(v[n], v[P - n]);
+        d[n - 1] = csub(v[n], v[P - n]);
+        sum = cadd(sum, s[n - 1]);
+    }
+    OddOut<P, INV, 1, H>::run(x0, s, d, v);
+    v[0] = sum;
+}
+
+template <int P, bool INV>
+__device__ __forceinline__ void dft(vec2_t* v) {
+    if constexpr (P == 2) dft2<INV>(v[0], v[1]);
+    else if constexpr (P == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else if constexpr (P == 8) dft8<INV>(v);
+    else if constexpr (P == 16) dft16<INV>(v);
+    else dft_odd<P, INV>(v);
+}
+
+// ---------------------------------------------------------------------------
+// the pass kernel
+// ---------------------------------------------------------------------------
+struct InnerStep {
+    FastDiv div_m, div_ns;
+    uint32_t m, ns, twstride;
+};
+
+template <int P, bool INV>
+__device__ __forceinline__ void inner_pass(const vec2_t* __restrict__ src, vec2_t* __restrict__ dst,
+                                           uint32_t R, uint32_t C, const InnerStep& st,
+                                           const vec2_t* __restrict__ tw) {
+    const uint32_t items = C * st.m;
+    for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
+        const uint32_t c = fdiv(it, st.div_m);
+        const uint32_t jj = it - c * st.m;
+        const uint32_t blk = fdiv(jj, st.div_ns);
+        const uint32_t kk = jj - blk * st.ns;
+        const uint32_t base = c * R;
+        vec2_t v[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) v[q] = src[pad(base + jj + q * st.m)];
+        if (st.ns > 1) {
+            const uint32_t step = kk * st.twstride;
+#pragma unroll
+            for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&tw[q * step]));
+        }
+        dft<P, INV>(v);
+        const uint32_t ob = base + blk * st.ns * P + kk;
+#pragma unroll
+        for (int q = 0; q < P; ++q) dst[pad(ob + q * st.ns)] = v[q];
+    }
+}
+
+template <bool INV, bool BIG>
+__device__ __forceinline__ void run_inner(int P, const vec2_t* src, vec2_t* dst, uint32_t R,
+                                          uint32_t C, const InnerStep& st, const vec2_t* tw) {
+    if constexpr (BIG) {
+        switch (P) {
+            case 17: inner_pass<17, INV>(src, dst, R, C, st, tw); return;
+            case 19: inner_pass<19, INV>(src, dst, R, C, st, tw); return;
+            case 23: inner_pass<23, INV>(src, dst, R, C, st, tw); return;
+            case 29: inner_pass<29, INV>(src, dst, R, C, st, tw); return;
+            case 31: inner_pass<31, INV>(src, dst, R, C, st, tw); return;
+            default: break;
+        }
+    }
+    switch (P) {
+        case 2: inner_pass<2, INV>(src, dst, R, C, st, tw); break;
+        case 3: inner_pass<3, INV>(src, dst, R, C, st, tw); break;
+        case 4: inner_pass<4, INV>(src, dst, R, C, st, tw); break;
+        case 5: inner_pass<5, INV>(src, dst, R, C, st, tw); break;
+        case 7: inner_pass<7, INV>(src, dst, R, C, st, tw); break;
+        case 8: inner_pass<8, INV>(src, dst, R, C, st, tw); break;
+        case 11: inner_pass<11, INV>(src, dst, R, C, st, tw); break;
+        case 13: inner_pass<13, INV>(src, dst, R, C, st, tw); break;
+        case 16: inner_pass<16, INV>(src, dst, R, C, st, tw); break;
+        default: break;
+    }
+}
+
+__device__ __forceinline__ vec2_t load_elem(const PassDesc& d, uint32_t b, uint32_t n) {
+    switch (d.pro_op) {
+        case PRO_CHIRP:
+            if (n < d.pro_bound)
+                return cmul(__ldcg(&d.in[b * d.in_bs + uint64_t(n) * d.in_es]), __ldg(&d.pro_tab[n]));
+            return {real_t(0), real_t(0)};
+        case PRO_GATHER:
+            return __ldcg(&d.in[b * d.in_bs + uint64_t(__ldg(&d.pro_perm[n])) * d.in_es]);
+        default:
+            return __ldcg(&d.in[b * d.in_bs + uint64_t(n) * d.in_es]);
+    }
+}
+
+__device__ __forceinline__ void store_elem(const PassDesc& d, uint32_t b, uint32_t k, vec2_t v) {
+    switch (d.epi_op) {
+        case EPI_MUL:
+            d.out[b * d.out_bs + uint64_t(k) * d.out_es] = cmul(v, __ldg(&d.epi_tab[k]));
+            break;
+        case EPI_CHIRP:
+            if (k < d.epi_bound)
+                d.out[b * d.out_bs + uint64_t(k) * d.out_es] =
+                    cscale(cmul(v, __ldg(&d.epi_tab[k])), d.scale);
+            break;
+        case EPI_RADER_FWD:
+            // spectrum of the gathered sequence times the kernel spectrum; bin 0
+            // is sum_{n>=1} x_n, so X_0 = x_0 + v is saved with x_0 per sequence
+            d.out[b * d.out_bs + uint64_t(k) * d.out_es] = cmul(v, __ldg(&d.epi_tab[k]));
+            if (k == 0) {
+                const vec2_t x0 = __ldcg(&d.aux_in[b * d.aux_in_bs]);
+                d.aux_out[2 * uint64_t(b)] = x0;
+                d.aux_out[2 * uint64_t(b) + 1] = cadd(x0, v);
+            }
+            break;
+        case EPI_RADER_INV: {
+            // X[g^-k] = x_0 + c_k, and X_0 from the saved pair; never reads the input,
+            // so the transform may run in place
+            const vec2_t x0 = __ldcg(&d.aux_in[2 * uint64_t(b)]);
+            const uint32_t idx = __ldg(&d.epi_perm[k]);
+            vec2_t* o = d.aux_out + b * d.aux_out_bs;
+            o[uint64_t(idx) * d.aux_out_es] = cscale(cadd(v, x0), d.scale);
+            if (k == 0) o[0] = cscale(__ldcg(&d.aux_in[2 * uint64_t(b) + 1]), d.scale);
+            break;
+        }
+        default:
+            d.out[b * d.out_bs + uint64_t(k) * d.out_es] = cscale(v, d.scale);
+            break;
+    }
+}
+
+struct PassExtra {
+    InnerStep step[kMaxInnerRadices];
+};
+
+PassExtra make_extra(const PassDesc& d);
+
+// One tile of one pass: C lanes of the length-R sub-FFT, shared-memory staged.
+template <bool INV, bool BIG>
+__device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x, uint32_t tile,
+                                          vec2_t* bufA) {
+    const uint32_t tile_elems = d.C * d.R;
+    vec2_t* bufB = bufA + pad(tile_elems) + 1;
+    const uint32_t total_lanes = d.batch * d.lanes_j;
+    const uint32_t lane0 = tile * d.C;
+
+    // ---- load: kLoadUnroll independent loads per thread in flight ---------
+    for (uint32_t base = threadIdx.x; base < tile_elems; base += kLoadUnroll * blockDim.x) {
+        vec2_t v[kLoadUnroll];
+        uint32_t slot[kLoadUnroll];
+        uint32_t twe[kLoadUnroll];
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u) {
+            const uint32_t idx = base + u * blockDim.x;
+            v[u] = {real_t(0), real_t(0)};
+            slot[u] = 0xffffffffu;
+            twe[u] = 0;
+            if (idx >= tile_elems) continue;
+            uint32_t c, r;
+            if (d.load_mode == MODE_LANE) {
+                r = fdiv(idx, d.div_C);
+                c = idx - r * d.C;
+            } else {
+                c = fdiv(idx, d.div_R);
+                r = idx - c * d.R;
+            }
+            slot[u] = pad(c * d.R + r);
+            const uint32_t g = lane0 + c;
+            if (g < total_lanes) {
+                uint32_t b, j;
+                if (d.order == ORDER_J) {
+                    b = fdiv(g, d.div_lanes_j);
+                    j = g - b * d.lanes_j;
+                } else {
+                    j = fdiv(g, d.div_batch);
+                    b = g - j * d.batch;
+                }
+                v[u] = load_elem(d, b, j + r * d.lanes_j);
+                if (d.Ns > 1) {
+                    const uint32_t kq = fdiv(j, d.div_Ns);
+                    const uint32_t k = j - kq * d.Ns;
+                    twe[u] = uint32_t(uint64_t(r) * k * d.tw_mul);
+                }
+            }
+        }
+        if (d.Ns > 1) {
+            const uint32_t mask = (1u << d.tw_shift) - 1u;
+#pragma unroll
+            for (int u = 0; u < kLoadUnroll; ++u) {
+                const vec2_t w = cmul(__ldg(&d.tw_hi[twe[u] >> d.tw_shift]), __ldg(&d.tw_lo[twe[u] & mask]));
+                v[u] = cmul(v[u], w);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u)
+            if (slot[u] != 0xffffffffu) bufA[slot[u]] = v[u];
+    }
+    __syncthreads();
+
+    // ---- inner sub-FFT of length R ------------------------------------
+    vec2_t* src = bufA;
+    vec2_t* dst = bufB;
+    for (int p = 0; p < d.nrad; ++p) {
+        run_inner<INV, BIG>(d.rad[p], src, dst, d.R, d.C, x.step[p], d.tw_inner);
+        __syncthreads();
+        vec2_t* t = src;
+        src = dst;
+        dst = t;
+    }
+
+    // ---- store ----------------------------------------------------------
+    for (uint32_t idx = threadIdx.x; idx < tile_elems; idx += blockDim.x) {
+        uint32_t c, r;
+        if (d.store_mode == MODE_LANE) {
+            r = fdiv(idx, d.div_C);
+            c = idx - r * d.C;
+        } else {
+            c = fdiv(idx, d.div_R);
+            r = idx - c * d.R;
+        }
+        const uint32_t g = lane0 + c;
+        if (g >= total_lanes) continue;
+        uint32_t b, j;
+        if (d.order == ORDER_J) {
+            b = fdiv(g, d.div_lanes_j);
+            j = g - b * d.lanes_j;
+        } else {
+            j = fdiv(g, d.div_batch);
+            b = g - j * d.batch;
+        }
+        const uint32_t blk = fdiv(j, d.div_Ns);
+        const uint32_t k = j - blk * d.Ns;
+        const uint32_t outk = blk * d.Ns * d.R + k + r * d.Ns;
+        store_elem(d, b, outk, src[pad(c * d.R + r)]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// register-resident tile: each inner pass moves its butterflies' values
+// through registers; the first pass reads global memory directly (with the
+// prologue and the outer twiddle), the last writes global memory directly
+// (with the epilogue), and only the exchanges between inner passes go through
+// one shared-memory buffer (read all, barrier, write all, barrier).
+// ---------------------------------------------------------------------------
+enum : int { IO_SMEM = 0, IO_GLOBAL = 1 };
+
+// Loads the P inputs of one butterfly of the first inner pass straight from
+// global memory: prologue, then the outer twiddle W_{Ns*R}^{r*k} (applied in
+// groups of four to bound the registers held by table loads).
+template <int P>
+__device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint32_t j, uint32_t jj,
+                                           uint32_t m, vec2_t* v) {
+    const uint64_t base = uint64_t(bs) * d.in_bs;
+    const uint64_t step = uint64_t(m) * d.lanes_j * d.in_es;
+    const uint64_t first = uint64_t(j + jj * d.lanes_j) * d.in_es;
+    switch (d.pro_op) {
+        case PRO_CHIRP:
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const uint32_t n = j + (jj + q * m) * d.lanes_j;
+                v[q] = (n < d.pro_bound) ? cmul(__ldcg(&d.in[base + first + q * step]), __ldg(&d.pro_tab[n]))
+                                         : vec2_t{real_t(0), real_t(0)};
+            }
+            break;
+        case PRO_GATHER:
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const uint32_t n = j + (jj + q * m) * d.lanes_j;
+                v[q] = __ldcg(&d.in[base + uint64_t(__ldg(&d.pro_perm[n])) * d.in_es]);
+            }
+            break;
+        default:
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[q] = __ldcg(&d.in[base + first + q * step]);
+            break;
+    }
+    if (d.Ns > 1) {
+        const uint32_t kq = fdiv(j, d.div_Ns);
+        const uint32_t k = j - kq * d.Ns;
+        const uint32_t mask = (1u << d.tw_shift) - 1u;
+        const uint32_t e0 = uint32_t(uint64_t(jj) * k * d.tw_mul);
+        const uint32_t es = uint32_t(uint64_t(m) * k * d.tw_mul);
+#pragma unroll
+        for (int g = 0; g < P; g += 4) {
+            vec2_t w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (g + u < P) {
+                    const uint32_t e = e0 + uint32_t(g + u) * es;  // < N, no wrap
+                    w[u] = cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
+                }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (g + u < P) v[g + u] = cmul(v[g + u], w[u]);
+        }
+    }
+}
+
+// Stores the P outputs of one butterfly of the last inner pass straight to
+// global memory through the epilogue.
+template <int P>
+__device__ __forceinline__ void fused_store(const PassDesc& d, uint32_t bs, uint32_t j, uint32_t ob,
+                                            uint32_t ns, const vec2_t* v) {
+    const uint32_t blo = fdiv(j, d.div_Ns);
+    const uint32_t ko = j - blo * d.Ns;
+    const uint32_t base = blo * d.Ns * d.R + ko;
+    if (d.epi_op == EPI_NONE) {
+        vec2_t* o = d.out + uint64_t(bs) * d.out_bs;
+        const uint64_t es = d.out_es;
+#pragma unroll
+        for (int q = 0; q < P; ++q) o[uint64_t(base + (ob + q * ns) * d.Ns) * es] = cscale(v[q], d.scale);
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; ++q) store_elem(d, bs, base + (ob + q * ns) * d.Ns, v[q]);
+    }
+}
+
+// One inner Stockham pass of radix P over the tile: each thread takes one
+// butterfly at a time from `src` (global memory on the first pass, else a
+// shared buffer) and writes it to `dst` (global memory on the last pass, else
+// the other shared buffer).
+template <int P, bool INV>
+__device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& st,
+                                           const vec2_t* src, vec2_t* dst, uint32_t lane0,
+                                           uint32_t total, int sio, int dio) {
+    const uint32_t m = st.m;
+    const uint32_t items = d.C * m;
+    const bool cfast = (sio == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
+                                          : ((dio == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
+    for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
+        uint32_t c, jj;
+        if (cfast) {
+            jj = fdiv(it, d.div_C);
+            c = it - jj * d.C;
+        } else {
+            c = fdiv(it, st.div_m);
+            jj = it - c * m;
+        }
+        const uint32_t g = lane0 + c;
+        uint32_t bs = 0, j = 0;
+        const bool live = g < total;
+        if ((sio == IO_GLOBAL || dio == IO_GLOBAL) && live) {
+            if (d.order == ORDER_J) {
+                bs = fdiv(g, d.div_lanes_j);
+                j = g - bs * d.lanes_j;
+            } else {
+                j = fdiv(g, d.div_batch);
+                bs = g - j * d.batch;
+            }
+        }
+        vec2_t v[P];
+        if (sio == IO_GLOBAL) {
+            if (live) {
+                fused_load<P>(d, bs, j, jj, m, v);
+            } else {
+#pragma unroll
+                for (int q = 0; q < P; ++q) v[q] = {real_t(0), real_t(0)};
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[q] = src[pad(c * d.R + jj + q * m)];
+        }
+        const uint32_t blk = fdiv(jj, st.div_ns);
+        const uint32_t kk = jj - blk * st.ns;
+        if (st.ns > 1) {
+            const uint32_t step = kk * st.twstride;
+#pragma unroll
+            for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&d.tw_inner[q * step]));
+        }
+        dft<P, INV>(v);
+        const uint32_t ob = blk * st.ns * P + kk;
+        if (dio == IO_SMEM) {
+#pragma unroll
+            for (int q = 0; q < P; ++q) dst[pad(c * d.R + ob + q * st.ns)] = v[q];
+        } else if (live) {
+            fused_store<P>(d, bs, j, ob, st.ns, v);
+        }
+    }
+}
+
+template <bool INV>
+__device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
+                                               const vec2_t* src, vec2_t* dst, uint32_t lane0,
+                                               uint32_t total, int sio, int dio) {
+    switch (P) {
+        case 2: fused_pass<2, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 3: fused_pass<3, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 4: fused_pass<4, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 5: fused_pass<5, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 7: fused_pass<7, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 8: fused_pass<8, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 11: fused_pass<11, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 13: fused_pass<13, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 16: fused_pass<16, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        default: break;
+    }
+}
+
+// A tile whose first inner pass reads global memory and whose last writes it:
+// two shared-memory round trips fewer than tile_body.  Shared memory holds two
+// buffers of pad(C*R)+1 elements (only when the sub-FFT has 3+ inner passes;
+// one buffer for 2 passes; none for 1).
+template <bool INV>
+__device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra& x, uint32_t tile,
+                                              vec2_t* sm) {
+    const uint32_t total = d.batch * d.lanes_j;
+    const uint32_t lane0 = tile * d.C;
+    const int np = d.nrad;
+    if (np == 0) {  // length-1 sub-FFT: the pass is a scaled copy (with its fused ops)
+        for (uint32_t c = threadIdx.x; c < d.C; c += blockDim.x) {
+            const uint32_t g = lane0 + c;
+            if (g >= total) continue;
+            uint32_t bs, j;
+            if (d.order == ORDER_J) {
+                bs = fdiv(g, d.div_lanes_j);
+                j = g - bs * d.lanes_j;
+            } else {
+                j = fdiv(g, d.div_batch);
+                bs = g - j * d.batch;
+            }
+            store_elem(d, bs, j, load_elem(d, bs, j));
+        }
+        return;
+    }
+    vec2_t* bufA = sm;
+    vec2_t* bufB = sm + pad(d.C * d.R) + 1;
+    const vec2_t* src = nullptr;
+    for (int p = 0; p < np; ++p) {
+        const bool last = (p + 1 == np);
+        vec2_t* dst = last ? nullptr : ((p % 2 == 0) ? bufA : bufB);
+        fused_dispatch<INV>(d.rad[p], d, x.step[p], src, dst, lane0, total,
+                            p == 0 ? IO_GLOBAL : IO_SMEM, last ? IO_GLOBAL : IO_SMEM);
+        if (!last) __syncthreads();
+        src = dst;
+    }
+}
+
+// ---- persistent-queue helpers --------------------------------------------
+struct QueueItem {
+    uint32_t desc;
+    uint32_t tile;
+};
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Waits for all tiles of pass `dep` to finish; a bounded spin that reports
+// failure instead of hanging.
+__device__ __forceinline__ bool wait_for(const uint32_t* done, uint32_t need) {
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
+        if (load_acquire(done) >= need) return true;
+        __nanosleep(200);
+    }
+    return false;
+}
+
+PassExtra make_extra(const PassDesc& d);
+
+}  // namespace kfft

@@ -1,0 +1,85 @@
+// persistent.cu -- the persistent work-queue kernel: one launch drains a
+// queue of (pass, tile) items ordered by dependency level, with bounded waits
+// on per-pass tile counters (a wait that gives up sets an error word).
+#include "fft_device.cuh"
+
+namespace kfft {
+
+__global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent(
+    const PassDesc* __restrict__ descs, const PassExtra* __restrict__ extras,
+    const int32_t* __restrict__ deps, const QueueItem* __restrict__ items, uint32_t nitems,
+    uint32_t* head, uint32_t* done, uint32_t* error) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_ok;
+    __shared__ __align__(16) PassDesc s_desc;
+    __shared__ __align__(16) PassExtra s_extra;
+    vec2_t* buf = reinterpret_cast<vec2_t*>(smem_raw);
+    while (true) {
+        if (threadIdx.x == 0) s_item = atomicAdd(head, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= nitems) return;
+        const QueueItem q = items[it];
+        if (threadIdx.x == 0) {
+            bool ok = true;
+            const int32_t dep = deps[q.desc];
+            if (dep >= 0) ok = wait_for(&done[dep], descs[dep].tiles);
+            if (!ok) atomicExch(error, 1u);
+            s_ok = ok ? 1u : 0u;
+        }
+        // stage the descriptor in shared memory
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&descs[q.desc]);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_desc);
+            for (uint32_t i = threadIdx.x; i < sizeof(PassDesc) / 4; i += blockDim.x) dst[i] = src[i];
+            const uint32_t* xs = reinterpret_cast<const uint32_t*>(&extras[q.desc]);
+            uint32_t* xd = reinterpret_cast<uint32_t*>(&s_extra);
+            for (uint32_t i = threadIdx.x; i < sizeof(PassExtra) / 4; i += blockDim.x) xd[i] = xs[i];
+        }
+        __syncthreads();
+        if (s_ok) {
+            if (s_desc.inv) tile_body_reg<true>(s_desc, s_extra, q.tile, buf);
+            else tile_body_reg<false>(s_desc, s_extra, q.tile, buf);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(&done[q.desc], 1u);
+    }
+}
+
+bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
+                       const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
+                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st) {
+    static int blocks_per_sm = -1;
+    static uint32_t configured_smem = 0;
+    static int sms = 0;
+    if (configured_smem < smem_bytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem_bytes));
+        if (e != cudaSuccess) {
+            note_cuda_error(e);
+            return false;
+        }
+        configured_smem = smem_bytes;
+        blocks_per_sm = -1;
+    }
+    if (blocks_per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_persistent, kPassThreads,
+                                                      smem_bytes);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    uint32_t grid = uint32_t(sms * blocks_per_sm);
+    if (grid > nitems) grid = nitems ? nitems : 1;
+    k_persistent<<<grid, kPassThreads, smem_bytes, st>>>(
+        descs, static_cast<const PassExtra*>(extras), deps, static_cast<const QueueItem*>(items),
+        nitems, head, done, error);
+    note_cuda_error(cudaGetLastError());
+    count_launch();
+    return true;
+}
+
+}  // namespace kfft

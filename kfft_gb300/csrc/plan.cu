@@ -114,6 +114,24 @@ static uint64_t next_smooth(uint64_t n) {
     return best;
 }
 
+// lanes of a multi-pass register-resident tile
+constexpr uint32_t kRegLanes = 4;
+
+// inner radix schedule of a tile length R: 16s first, then 8/4/2, then odd primes
+static std::vector<uint8_t> inner_radices(uint32_t R);
+
+// true when a tile of C lanes of length R fits the fused-I/O kernel: every
+// inner radix <= 16 and at most kRegTile points per tile
+static bool reg_tile_fits(uint32_t R, uint32_t C) {
+    if (C < 1 || uint64_t(C) * R > kRegTile) return false;
+    if (R == 1) return true;  // a length-1 pass is a copy
+    std::vector<uint8_t> rad = inner_radices(R);
+    if (rad.empty() || rad.size() > size_t(kMaxInnerRadices)) return false;
+    for (uint8_t r : rad)
+        if (r > 16) return false;
+    return true;
+}
+
 // inner radix schedule of a tile length R: 16s first, then 8/4/2, then odd primes
 static std::vector<uint8_t> inner_radices(uint32_t R) {
     std::vector<uint8_t> r;
@@ -203,8 +221,28 @@ FftPlan::~FftPlan() {
 static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     const uint32_t N = P->N;
     std::vector<uint32_t> Rs;
-    if (N <= tile_capacity()) Rs.push_back(N);
-    else Rs = split_passes(N, kMultiRmax);
+    // lengths whose radices are all <= 16 run in register-resident tiles (one
+    // pass when the whole sequence fits, else the largest balanced split whose
+    // tiles of kRegLanes lanes fit); others use the shared-memory ping-pong tile
+    bool small_radices = true;
+    for (uint32_t f : prime_factors(N)) small_radices = small_radices && f <= 13;
+    if (small_radices && reg_tile_fits(N, 1)) {
+        Rs.push_back(N);
+    } else if (small_radices) {
+        for (uint32_t rmax : {1024u, 768u, 512u, 384u, 256u, 128u, 64u, 32u, 16u}) {
+            std::vector<uint32_t> cand = split_passes(N, rmax);
+            bool ok = !cand.empty();
+            for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R));
+            if (ok) {
+                Rs = cand;
+                break;
+            }
+        }
+    }
+    if (Rs.empty()) {
+        if (N <= tile_capacity()) Rs.push_back(N);
+        else Rs = split_passes(N, kMultiRmax);
+    }
     if (Rs.empty()) return false;
     std::map<uint32_t, const vec2_t*> inner;
     uint32_t Ns = 1;
@@ -449,14 +487,37 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
     }
     if (C < 1) C = 1;
+    // register-resident tile when every inner radix is <= 16 and each thread's
+    // share of every inner pass fits its register budget (lower C if needed)
+    {
+        bool radix_ok = !s.radices.empty() || s.R == 1;
+        for (uint8_t r : s.radices) radix_ok = radix_ok && r <= 16;
+        for (uint32_t c = C; radix_ok && c >= 1; --c) {
+            const bool fits = reg_tile_fits(s.R, c);
+            const bool coalesced_enough = (d.order == ORDER_J && d.lanes_j == 1) ||
+                                          c >= std::min<uint32_t>(C, kRegLanes);
+            if (fits && coalesced_enough) {
+                C = c;
+                d.regmode = 1;
+                break;
+            }
+            if (!coalesced_enough) break;
+        }
+    }
     d.C = C;
     const uint64_t lanes = uint64_t(d.batch) * d.lanes_j;
     d.tiles = uint32_t((lanes + C - 1) / C);
     uint32_t elems = C * s.R;
-    uint32_t t = (elems + 7) / 8;
-    t = (t + 31) / 32 * 32;
-    d.threads = std::max<uint32_t>(64, std::min<uint32_t>(kPassThreads, t));
-    d.smem_bytes = smem_for(elems);
+    if (d.regmode) {
+        d.threads = kPassThreads;
+        const uint32_t nbuf = s.radices.size() >= 3 ? 2u : (s.radices.size() == 2 ? 1u : 0u);
+        d.smem_bytes = nbuf * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
+    } else {
+        uint32_t t = (elems + 7) / 8;
+        t = (t + 31) / 32 * 32;
+        d.threads = std::max<uint32_t>(64, std::min<uint32_t>(kPassThreads, t));
+        d.smem_bytes = smem_for(elems);
+    }
     d.div_R.init(s.R);
     d.div_lanes_j.init(d.lanes_j);
     d.div_batch.init(d.batch);

@@ -114,6 +114,8 @@ bool record(kfft_plan_uneven* P, const vec2_t* in, vec2_t* out) {
         }
     }
     const uint32_t nd = uint32_t(all.size());
+    for (const PassDesc& d : all)
+        if (!d.regmode) return false;  // the queue kernel runs register-resident tiles only
     std::vector<Item> items;
     uint32_t smem = 0;
     for (uint32_t d = 0; d < nd; ++d) {
