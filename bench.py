@@ -103,12 +103,16 @@ class Workload:
 class Uniform(Workload):
     """B complex sequences of one length N, forward then inverse per step."""
 
-    def __init__(self, lib, N, B, precision, seed, dist_name):
+    def __init__(self, lib, N, B, precision, seed, dist_name, tc=False):
         self.lib = lib
         self.N, self.B, self.precision, self.seed = N, B, precision, seed
         self.dist_name = dist_name
+        self.tc = tc and precision == "float"
         tag = "fp64" if precision == "double" else "fp32"
-        self.name = f"c2c {tag} N={N} batch {B} forward+inverse"
+        self.name = f"c2c {tag} N={N} batch {B} forward+inverse" + (
+            ", radix-16 stages on tensor cores (FP16 split hi+lo, FP32 accumulate)" if self.tc else "")
+        if dist_name == "hdr":
+            self.name += ", high-dynamic-range input"
 
     def _cdt(self):
         return np.complex128 if self.precision == "double" else np.complex64
@@ -118,6 +122,17 @@ class Uniform(Workload):
         shape = (self.B, self.N)
         if self.dist_name == "uniform":
             x = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        elif self.dist_name == "hdr":
+            # 32 random tones, amplitudes log-uniform 1e-6..1, random phases, + N(0, 1e-7^2)
+            n = np.arange(self.N)
+            x = np.zeros(shape, np.complex128)
+            for b_ in range(self.B):
+                f = rng.integers(0, self.N, 32)
+                amp = 10.0 ** rng.uniform(-6, 0, 32)
+                ph = rng.uniform(0, 2 * np.pi, 32)
+                for k in range(32):
+                    x[b_] += amp[k] * np.exp(1j * (2 * np.pi * f[k] * n / self.N + ph[k]))
+            x += 1e-7 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
         else:
             x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
         return x.astype(self._cdt())
@@ -125,8 +140,9 @@ class Uniform(Workload):
     def setup(self, torch, dev, nbuf):
         x = self._input()
         self.host_in = x
-        self.fwd = self.lib.L.kfft_config_cpx(self.N, 0, None, None)
-        self.inv = self.lib.L.kfft_config_cpx(self.N, 1, None, None)
+        extra = (1 << 8) if self.tc else 0  # KFFT_FLAG_TENSOR_CORES
+        self.fwd = self.lib.L.kfft_config_cpx(self.N, 0 | extra, None, None)
+        self.inv = self.lib.L.kfft_config_cpx(self.N, 1 | extra, None, None)
         assert self.fwd and self.inv, self.lib.last_error()
         # rotating input buffers: together larger than the 129 MB L2
         self.ins = [torch.from_numpy(x).to(dev) for _ in range(nbuf)]
@@ -172,6 +188,16 @@ class Uniform(Workload):
         b = self.bytes_per_buffer()
         return 2 * b, 2 * b
 
+    def accuracy(self, oracle_mod, max_seq=4):
+        """rel-L2 of the forward transform against the FP64 oracle on the same input."""
+        k = min(self.B, max_seq)
+        x = np.ascontiguousarray(self.host_in[:k])
+        y = np.empty_like(x)
+        assert self.lib.L.kfft_eval_cpx_batch(self.fwd, x.ctypes.data, y.ctypes.data, k) == 0
+        ref = oracle_mod.fft_cpx(x.astype(np.complex128))
+        return {"rel_l2_vs_fp64_oracle": float(np.linalg.norm(y - ref) / np.linalg.norm(ref)),
+                "sequences_checked": int(k), "input": self.dist_name}
+
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
         fwd = oracle_mod.CpxPlan(self.N, 0)
         inv = oracle_mod.CpxPlan(self.N, 1)
@@ -194,6 +220,10 @@ def C2C4096(lib):
 
 
 UNIFORM_WORKLOADS = {
+    "tc_f32_2p18x64": lambda lib: Uniform(lib, 1 << 18, 64, "float", 3, "normal", tc=True),
+    "tc_f32_2p24": lambda lib: Uniform(lib, 1 << 24, 1, "float", 3, "normal", tc=True),
+    "tc_f32_2p18x64_hdr": lambda lib: Uniform(lib, 1 << 18, 64, "float", 4, "hdr", tc=True),
+    "c2c_f32_2p18x64_hdr": lambda lib: Uniform(lib, 1 << 18, 64, "float", 4, "hdr"),
     "c2c4096": lambda lib: Uniform(lib, 4096, 256, "double", 1, "uniform"),
     "c2c_f32_2p18x64": lambda lib: Uniform(lib, 1 << 18, 64, "float", 3, "normal"),
     "c2c_f32_2p24": lambda lib: Uniform(lib, 1 << 24, 1, "float", 3, "normal"),
@@ -480,6 +510,9 @@ def main():
             "e2e": {"value": round(e2e_val, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
             "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary()}
+    if rank == 0 and hasattr(wl, "accuracy"):
+        from oracle import oracle as _oracle
+        line["accuracy"] = wl.accuracy(_oracle)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
         threads = os.cpu_count() or 1

@@ -202,6 +202,25 @@ KFFT_API kfft_return_t kfft_cleanup(void* mem);
     } while (0)
 KFFT_API const char* kfft_strerr(const kfft_return_t code);
 
+/* ---- incs/kfft_shift.h:16-27: fftshift (forward) / ifftshift (inverse) ---- */
+KFFT_API void kfft_shift_cpx(kfft_cpx* buf, const uint32_t size, const bool is_inverse,
+                             kfft_pool_t* mmgr);
+KFFT_API void kfft_shift_scalar(kfft_scalar* buf, const uint32_t size, const bool is_inverse,
+                                kfft_pool_t* mmgr);
+
+/* ---- incs/kfft_math.h:251-350: element-wise and layout helpers ----------- */
+KFFT_API void kfft_math_hadamard_cpx(kfft_cpx* Fout, const kfft_cpx* Fin, uint32_t size);
+KFFT_API void kfft_math_hadamard_scalar(kfft_scalar* Fout, const kfft_scalar* Fin, uint32_t size);
+KFFT_API void kfft_math_transpose_cpx(const kfft_cpx* Fin, kfft_cpx* Fout, const uint32_t x,
+                                      const uint32_t y);
+KFFT_API void kfft_math_transpose_scalar(const kfft_scalar* Fin, kfft_scalar* Fout,
+                                         const uint32_t x, const uint32_t y);
+KFFT_API void kfft_math_transpose_ip_cpx(kfft_cpx* Fin, const uint32_t x, const uint32_t y);
+KFFT_API void kfft_math_transpose_ip_scalar(kfft_scalar* Fin, const uint32_t x, const uint32_t y);
+KFFT_API void kfft_math_magnitude(const kfft_cpx* Fin, kfft_scalar* Fout, uint32_t size);
+KFFT_API void kfft_math_magnitude_ip(kfft_cpx* Fin, uint32_t size);
+KFFT_API kfft_scalar kfft_math_average(const kfft_scalar* Fin, uint32_t size);
+
 /* ---- ext/2d/kfft_cpx2.h:3-17, ext/2d/kfft_scalar2.h:3-19 ----------------- */
 typedef struct {
     kfft_object_t object;
@@ -216,6 +235,8 @@ typedef struct {
 KFFT_API kfft_plan_c2d* kfft_config2_cpx(const uint32_t x_size, const uint32_t y_size,
                                          const uint32_t flags, kfft_pool_t* A, size_t* lenmem);
 KFFT_API kfft_return_t kfft_eval2_cpx(kfft_plan_c2d* cfg, const kfft_cpx* fin, kfft_cpx* fout);
+KFFT_API void kfft_shift2_cpx(kfft_cpx* buf, kfft_cpx* ftmp, const uint32_t sz_x,
+                              const uint32_t sz_y, const bool is_inverse, kfft_pool_t* mmgr);
 
 typedef struct {
     kfft_object_t object;
@@ -233,6 +254,8 @@ KFFT_API kfft_return_t kfft_eval2_scalar(kfft_plan_s2d* plan, const kfft_scalar*
                                          kfft_cpx* fout);
 KFFT_API kfft_return_t kfft_evali2_scalar(kfft_plan_s2d* plan, const kfft_cpx* fin,
                                           kfft_scalar* fout);
+KFFT_API void kfft_shift2_scalar(kfft_scalar* buf, kfft_scalar* ftmp, const uint32_t sz_x,
+                                 const uint32_t sz_y, const bool is_inverse, kfft_pool_t* mmgr);
 
 /* ---- ext/conv/kfft_cpx_conv.h:5-21, ext/conv/kfft_scalar_conv.h:5-19 ----- */
 typedef struct {

@@ -17,6 +17,13 @@ extern "C" {
 #endif
 
 /*
+ * Plan flag (additive, above the reference's bits 0-5): in the float build,
+ * run the radix-16 stages of direct plans as FP16 split hi+lo matrix products
+ * on tensor cores with FP32 accumulation.  Ignored by the double build.
+ */
+#define KFFT_FLAG_TENSOR_CORES (1u << 8)
+
+/*
  * Batched complex transform: `batch` sequences of plan->nfft points stored back
  * to back.  fin/fout may be host or device memory (fin == fout allowed).
  * Synchronous, like kfft_eval_cpx.  Same return codes as kfft_eval_cpx.

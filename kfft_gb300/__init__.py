@@ -52,6 +52,10 @@ EXPORTED_SYMBOLS = [
     "kfft_uneven_total", "kfft_release_uneven",
     "kfft_gb300_stats", "kfft_gb300_last_error", "kfft_gb300_describe",
     "kfft_eval_cpx_noalloc", "kfft_noalloc_scratch_bytes", "kfft_noalloc_last_message",
+    "kfft_shift_cpx", "kfft_shift_scalar", "kfft_shift2_cpx", "kfft_shift2_scalar",
+    "kfft_math_hadamard_cpx", "kfft_math_hadamard_scalar", "kfft_math_transpose_cpx",
+    "kfft_math_transpose_scalar", "kfft_math_transpose_ip_cpx", "kfft_math_transpose_ip_scalar",
+    "kfft_math_magnitude", "kfft_math_magnitude_ip", "kfft_math_average",
 ]
 
 
@@ -150,6 +154,19 @@ class KfftLib:
         L.kfft_eval_cpx_noalloc.argtypes = [vp, vp, vp, u32, vp]
         L.kfft_noalloc_scratch_bytes.restype = sz
         L.kfft_noalloc_last_message.restype = ctypes.c_char_p
+        for n in ("kfft_shift_cpx", "kfft_shift_scalar"):
+            getattr(L, n).argtypes = [vp, u32, ctypes.c_bool, vp]
+        for n in ("kfft_shift2_cpx", "kfft_shift2_scalar"):
+            getattr(L, n).argtypes = [vp, vp, u32, u32, ctypes.c_bool, vp]
+        for n in ("kfft_math_hadamard_cpx", "kfft_math_hadamard_scalar", "kfft_math_magnitude"):
+            getattr(L, n).argtypes = [vp, vp, u32]
+        for n in ("kfft_math_transpose_cpx", "kfft_math_transpose_scalar"):
+            getattr(L, n).argtypes = [vp, vp, u32, u32]
+        for n in ("kfft_math_transpose_ip_cpx", "kfft_math_transpose_ip_scalar"):
+            getattr(L, n).argtypes = [vp, u32, u32]
+        L.kfft_math_magnitude_ip.argtypes = [vp, u32]
+        L.kfft_math_average.argtypes = [vp, u32]
+        L.kfft_math_average.restype = ctypes.c_float if precision == "float" else ctypes.c_double
         L.kfft_gb300_last_error.restype = ctypes.c_char_p
         L.kfft_gb300_describe.restype = ctypes.c_char_p
         L.kfft_gb300_describe.argtypes = [vp]

@@ -372,6 +372,9 @@ bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm) 
     cudaStream_t st = sync_stream();
     g->plan = make_plan(nfft, sign, *g->arena, st);
     if (!g->plan) return false;
+#if defined(KFFT_HALF_SCALAR)
+    set_tensor_cores(g->plan, (flags & KFFT_FLAG_TENSOR_CORES) != 0);
+#endif
     if (finish(st) != KFFT_RET_SUCCESS) return false;
     P->gpu = g;
     const FftPlan& fp = *g->plan;

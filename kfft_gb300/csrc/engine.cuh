@@ -85,6 +85,7 @@ struct PassDesc {
     uint8_t load_mode, store_mode, order;
     uint8_t inv;             // butterfly direction (tables already carry it)
     uint8_t regmode;         // fused-I/O tile (radices <= 16, C*R <= kRegTile)
+    uint8_t tc;              // radix-16 inner passes on tensor cores (FP32 build)
     uint8_t nrad;
     uint8_t rad[kMaxInnerRadices];
     FastDiv div_R, div_lanes_j, div_batch, div_Ns, div_C;
@@ -171,6 +172,7 @@ struct DeviceArena;  // device memory owned by a plan tree
 struct FftPlan {
     uint32_t N = 0;
     int sign = -1;  // -1 forward, +1 inverse
+    bool tc = false;  // radix-16 passes on tensor cores (FP32 build)
     Method method = METHOD_DIRECT;
     // DIRECT
     std::vector<PassSpec> passes;
@@ -217,6 +219,8 @@ struct DeviceArena {
 FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
                    uint32_t max_prime = kMaxDirectPrime);
 bool is_direct_length(uint32_t n, uint32_t max_prime = kMaxDirectPrime);
+// Marks a plan tree to run its radix-16 passes on tensor cores (FP32 build).
+void set_tensor_cores(FftPlan* p, bool on);
 std::string describe(const FftPlan& p);
 // Device workspace (bytes) the plan needs for `batch` sequences.
 size_t workspace_bytes(const FftPlan& p, uint32_t batch);

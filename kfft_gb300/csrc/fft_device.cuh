@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cuda_fp16.h>
+
 #include <cstring>
 
 #include "engine.cuh"
@@ -506,6 +508,39 @@ __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x,
 // ---------------------------------------------------------------------------
 enum : int { IO_SMEM = 0, IO_GLOBAL = 1 };
 
+// v[q] *= W^(q*step) for q = 1..P-1, W^i = tw[i].  FP64 loads every factor
+// (the FP64 pipe, not the loads, bounds it).  FP32 loads the four anchors
+// W^(step), W^(2 step), W^(4 step), W^(8 step) and forms the others as
+// products of at most four anchors: a quarter of the table loads, which were
+// the L1 bottleneck, for a few ulp of extra rounding.
+template <int P>
+__device__ __forceinline__ void apply_inner_twiddles(vec2_t* v, const vec2_t* __restrict__ tw,
+                                                     uint32_t step) {
+#if defined(KFFT_HALF_SCALAR)
+    if constexpr (P >= 4) {
+        vec2_t a[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            if ((1 << b) < P) a[b] = __ldg(&tw[(1u << b) * step]);
+#pragma unroll
+        for (int q = 1; q < P; ++q) {
+            vec2_t w = {real_t(1), real_t(0)};
+            bool first = true;
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+                if (q & (1 << b)) {
+                    w = first ? a[b] : cmul(w, a[b]);
+                    first = false;
+                }
+            v[q] = cmul(v[q], w);
+        }
+        return;
+    }
+#endif
+#pragma unroll
+    for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&tw[q * step]));
+}
+
 // Loads the P inputs of one butterfly of the first inner pass straight from
 // global memory: prologue, then the outer twiddle W_{Ns*R}^{r*k} (applied in
 // groups of four to bound the registers held by table loads).
@@ -542,6 +577,30 @@ __device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint3
         const uint32_t mask = (1u << d.tw_shift) - 1u;
         const uint32_t e0 = uint32_t(uint64_t(jj) * k * d.tw_mul);
         const uint32_t es = uint32_t(uint64_t(m) * k * d.tw_mul);
+#if defined(KFFT_HALF_SCALAR)
+        if constexpr (P >= 4) {
+            // FP32: W^(e0 + q es) from the base W^(e0) and the anchors W^(2^b es):
+            // ten table loads per butterfly instead of 2P (the L1 bottleneck)
+            auto tw2 = [&](uint32_t e) {
+                return cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
+            };
+            const vec2_t w0 = tw2(e0);
+            vec2_t a[4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+                if ((1 << b) < P) a[b] = tw2((1u << b) * es);
+            v[0] = cmul(v[0], w0);
+#pragma unroll
+            for (int q = 1; q < P; ++q) {
+                vec2_t w = w0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    if (q & (1 << b)) w = cmul(w, a[b]);
+                v[q] = cmul(v[q], w);
+            }
+            return;
+        }
+#endif
 #pragma unroll
         for (int g = 0; g < P; g += 4) {
             vec2_t w[4];
@@ -624,11 +683,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         }
         const uint32_t blk = fdiv(jj, st.div_ns);
         const uint32_t kk = jj - blk * st.ns;
-        if (st.ns > 1) {
-            const uint32_t step = kk * st.twstride;
-#pragma unroll
-            for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&d.tw_inner[q * step]));
-        }
+        if (st.ns > 1) apply_inner_twiddles<P>(v, d.tw_inner, kk * st.twstride);
         dft<P, INV>(v);
         const uint32_t ob = blk * st.ns * P + kk;
         if (dio == IO_SMEM) {
@@ -639,6 +694,207 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         }
     }
 }
+
+#if defined(KFFT_HALF_SCALAR)
+// ---------------------------------------------------------------------------
+// Tensor-core radix-16 (FP32 build): the 16-point DFT of 8 butterflies at a
+// time as a real 16x16 by 16x8 matrix product per real/imaginary part on
+// mma.sync.m16n8k16 (FP16 operands, FP32 accumulation).  Operands are split
+// into FP16 hi + lo parts and three products are summed (Fh*Xh + Fh*Xl +
+// Fl*Xh); each butterfly's inputs are scaled by a power of two so that their
+// largest component lies in [0.5, 1), which keeps the lo parts normal.
+// Fragment layout (PTX ISA, m16n8k16): lane = 4*g + t; A row-major 16x16:
+// a{0,1} = (g, 2t+{0,1}), a{2,3} = (g+8, 2t+{0,1}), a{4,5} = (g, 2t+8+{0,1}),
+// a{6,7} = (g+8, 2t+8+{0,1}); B col-major 16x8: b{0,1} = (2t+{0,1}, g),
+// b{2,3} = (2t+8+{0,1}, g); C 16x8: c{0,1} = (g, 2t+{0,1}), c{2,3} = (g+8, 2t+{0,1}).
+// ---------------------------------------------------------------------------
+struct TcFrag {
+    uint32_t hi[4], lo[4];
+};
+
+__device__ __forceinline__ uint32_t pack_half2(float a, float b) {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
+    const float ra = a - __half2float(ha), rb = b - __half2float(hb);
+    __half2 h2 = __halves2half2(ha, hb);
+    hi = *reinterpret_cast<uint32_t*>(&h2);
+    lo = pack_half2(ra, rb);
+}
+
+// A fragment of cos (part 0), s*sin (part 1) or -s*sin (part 2) of 2*pi*m*k/16,
+// s = -1 forward, +1 inverse
+template <bool INV>
+__device__ __forceinline__ TcFrag dft16_frag(int part) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int rows[4] = {g, g + 8, g, g + 8};
+    const int cols[4] = {2 * t, 2 * t, 2 * t + 8, 2 * t + 8};
+    TcFrag f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float v[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int mk = (rows[r] * (cols[r] + e)) & 15;
+            float s, c;
+            sincospif(float(mk) / 8.0f, &s, &c);
+            const float sgn = INV ? 1.0f : -1.0f;
+            v[e] = part == 0 ? c : (part == 1 ? sgn * s : -sgn * s);
+        }
+        split_pair(v[0], v[1], f.hi[r], f.lo[r]);
+    }
+    return f;
+}
+
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// acc += F * X with F = Fh + Fl and X = Xh + Xl (three products)
+__device__ __forceinline__ void mma_split(float* acc, const TcFrag& F, const uint32_t* xh,
+                                          const uint32_t* xl) {
+    mma16816(acc, F.hi, xh);
+    mma16816(acc, F.hi, xl);
+    mma16816(acc, F.lo, xh);
+}
+
+// One radix-16 inner pass on tensor cores.  Each warp takes butterflies in
+// groups of 8: lane 4g+t loads inputs k = 2t, 2t+1, 2t+8, 2t+9 of butterfly g
+// and, after the products, holds outputs g and g+8 of butterflies 2t, 2t+1.
+template <bool INV>
+__device__ __forceinline__ void tc_pass16(const PassDesc& d, const InnerStep& st,
+                                          const vec2_t* src, vec2_t* dst, uint32_t lane0,
+                                          uint32_t total, int sio, int dio, const TcFrag& Fr,
+                                          const TcFrag& Fi, const TcFrag& Gm) {
+    const uint32_t m = st.m;
+    const uint32_t items = d.C * m;
+    const int lane = threadIdx.x & 31, gq = lane >> 2, tq = lane & 3;
+    const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const bool cfast = (sio == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
+                                          : ((dio == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
+    const int ks[4] = {2 * tq, 2 * tq + 1, 2 * tq + 8, 2 * tq + 9};
+    for (uint32_t grp = warp; grp * 8 < items; grp += nwarps) {
+        // ---- inputs of butterfly gq --------------------------------------------
+        const uint32_t it = grp * 8 + gq;
+        vec2_t x[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (it < items) {
+            uint32_t c, jj;
+            if (cfast) {
+                jj = fdiv(it, d.div_C);
+                c = it - jj * d.C;
+            } else {
+                c = fdiv(it, st.div_m);
+                jj = it - c * m;
+            }
+            const uint32_t g = lane0 + c;
+            if (sio == IO_GLOBAL) {
+                if (g < total) {
+                    uint32_t bs, j;
+                    if (d.order == ORDER_J) {
+                        bs = fdiv(g, d.div_lanes_j);
+                        j = g - bs * d.lanes_j;
+                    } else {
+                        j = fdiv(g, d.div_batch);
+                        bs = g - j * d.batch;
+                    }
+                    const uint32_t kq = fdiv(j, d.div_Ns);
+                    const uint32_t kk = j - kq * d.Ns;
+                    const uint32_t mask = (1u << d.tw_shift) - 1u;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const uint32_t r = jj + uint32_t(ks[u]) * m;
+                        x[u] = load_elem(d, bs, j + r * d.lanes_j);
+                        if (d.Ns > 1) {
+                            const uint32_t e = uint32_t(uint64_t(r) * kk * d.tw_mul);
+                            x[u] = cmul(x[u], cmul(__ldg(&d.tw_hi[e >> d.tw_shift]),
+                                                   __ldg(&d.tw_lo[e & mask])));
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) x[u] = src[pad(c * d.R + jj + uint32_t(ks[u]) * m)];
+            }
+            if (st.ns > 1) {
+                const uint32_t blk = fdiv(jj, st.div_ns);
+                const uint32_t kk = jj - blk * st.ns;
+                const uint32_t step = kk * st.twstride;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ks[u]) x[u] = cmul(x[u], __ldg(&d.tw_inner[uint32_t(ks[u]) * step]));
+            }
+        }
+        // ---- per-butterfly power-of-two scale ---------------------------------
+        float mx = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) mx = fmaxf(mx, fmaxf(fabsf(x[u].x), fabsf(x[u].y)));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+        int ex = 0;
+        if (mx > 0.f) frexpf(mx, &ex);
+        const float sc = ldexpf(1.0f, -ex), inv_sc = ldexpf(1.0f, ex);
+        uint32_t xrh[2], xrl[2], xih[2], xil[2];
+        split_pair(x[0].x * sc, x[1].x * sc, xrh[0], xrl[0]);
+        split_pair(x[2].x * sc, x[3].x * sc, xrh[1], xrl[1]);
+        split_pair(x[0].y * sc, x[1].y * sc, xih[0], xil[0]);
+        split_pair(x[2].y * sc, x[3].y * sc, xih[1], xil[1]);
+        // ---- Yr = Fr Xr - Fi Xi, Yi = Fi Xr + Fr Xi ------------------------------
+        float yr[4] = {0.f, 0.f, 0.f, 0.f}, yi[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_split(yr, Fr, xrh, xrl);
+        mma_split(yr, Gm, xih, xil);
+        mma_split(yi, Fi, xrh, xrl);
+        mma_split(yi, Fr, xih, xil);
+        // ---- outputs g and g+8 of butterflies 2t and 2t+1 -------------------------
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t n = uint32_t(2 * tq + e);
+            const float un = __shfl_sync(0xffffffffu, inv_sc, int(n) * 4);
+            const uint32_t ito = grp * 8 + n;
+            if (ito >= items) continue;
+            uint32_t co, jo;
+            if (cfast) {
+                jo = fdiv(ito, d.div_C);
+                co = ito - jo * d.C;
+            } else {
+                co = fdiv(ito, st.div_m);
+                jo = ito - co * m;
+            }
+            const uint32_t blk = fdiv(jo, st.div_ns);
+            const uint32_t kk = jo - blk * st.ns;
+            const uint32_t ob = blk * st.ns * 16 + kk;
+            const vec2_t o0 = {yr[e] * un, yi[e] * un};          // output gq
+            const vec2_t o1 = {yr[2 + e] * un, yi[2 + e] * un};  // output gq + 8
+            if (dio == IO_SMEM) {
+                dst[pad(co * d.R + ob + uint32_t(gq) * st.ns)] = o0;
+                dst[pad(co * d.R + ob + uint32_t(gq + 8) * st.ns)] = o1;
+            } else {
+                const uint32_t g = lane0 + co;
+                if (g >= total) continue;
+                uint32_t bs, j;
+                if (d.order == ORDER_J) {
+                    bs = fdiv(g, d.div_lanes_j);
+                    j = g - bs * d.lanes_j;
+                } else {
+                    j = fdiv(g, d.div_batch);
+                    bs = g - j * d.batch;
+                }
+                const uint32_t blo = fdiv(j, d.div_Ns);
+                const uint32_t ko = j - blo * d.Ns;
+                const uint32_t base = blo * d.Ns * d.R + ko;
+                store_elem(d, bs, base + (ob + uint32_t(gq) * st.ns) * d.Ns, o0);
+                store_elem(d, bs, base + (ob + uint32_t(gq + 8) * st.ns) * d.Ns, o1);
+            }
+        }
+    }
+}
+#endif
 
 template <bool INV>
 __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
@@ -687,11 +943,24 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     vec2_t* bufA = sm;
     vec2_t* bufB = sm + pad(d.C * d.R) + 1;
     const vec2_t* src = nullptr;
+#if defined(KFFT_HALF_SCALAR)
+    TcFrag Fr, Fi, Gm;
+    if (d.tc) {
+        Fr = dft16_frag<INV>(0);
+        Fi = dft16_frag<INV>(1);
+        Gm = dft16_frag<INV>(2);
+    }
+#endif
     for (int p = 0; p < np; ++p) {
         const bool last = (p + 1 == np);
         vec2_t* dst = last ? nullptr : ((p % 2 == 0) ? bufA : bufB);
-        fused_dispatch<INV>(d.rad[p], d, x.step[p], src, dst, lane0, total,
-                            p == 0 ? IO_GLOBAL : IO_SMEM, last ? IO_GLOBAL : IO_SMEM);
+        const int sio = p == 0 ? IO_GLOBAL : IO_SMEM, dio = last ? IO_GLOBAL : IO_SMEM;
+#if defined(KFFT_HALF_SCALAR)
+        if (d.tc && d.rad[p] == 16)
+            tc_pass16<INV>(d, x.step[p], src, dst, lane0, total, sio, dio, Fr, Fi, Gm);
+        else
+#endif
+            fused_dispatch<INV>(d.rad[p], d, x.step[p], src, dst, lane0, total, sio, dio);
         if (!last) __syncthreads();
         src = dst;
     }

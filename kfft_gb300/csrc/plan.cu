@@ -401,6 +401,13 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
     return P;
 }
 
+void set_tensor_cores(FftPlan* p, bool on) {
+    if (!p) return;
+    p->tc = on;
+    set_tensor_cores(p->sub_fwd, on);
+    set_tensor_cores(p->sub_inv, on);
+}
+
 std::string describe(const FftPlan& p) {
     std::ostringstream o;
     const char* m[] = {"direct", "rader", "bluestein"};
@@ -466,6 +473,9 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     d.lanes_j = P.N / s.R;
     d.order = lin.order;
     d.inv = P.sign > 0 ? 1 : 0;
+#if defined(KFFT_HALF_SCALAR)
+    d.tc = P.tc ? 1 : 0;
+#endif
     d.nrad = uint8_t(s.radices.size());
     for (size_t i = 0; i < s.radices.size(); ++i) d.rad[i] = s.radices[i];
     const uint32_t cap = tile_capacity();

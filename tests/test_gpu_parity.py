@@ -276,3 +276,22 @@ def test_uneven_workload_subset(precision):
         worst = max(worst, e / (tol64(n) if precision == "double" else TOL32))
         off += n
     assert worst <= 1.0, worst
+
+
+@pytest.mark.parametrize("n,batch", [(16, 64), (256, 16), (4096, 8), (65536, 2), (1 << 18, 1),
+                                     (1 << 20, 1), (3 * 4096, 2), (1000, 4)])
+def test_tensor_core_radix16_path(libf, n, batch):
+    """FP32 build with KFFT_FLAG_TENSOR_CORES: FP16 split hi+lo radix-16 stages."""
+    rng = np.random.default_rng(n)
+    x = cx(rng, batch, n).astype(np.complex64)
+    ref = O.fft_cpx(x.astype(np.complex128))
+    p = libf.L.kfft_config_cpx(n, 1 << 8, None, None)
+    y = np.empty_like(x)
+    assert libf.L.kfft_eval_cpx_batch(p, x.ctypes.data, y.ctypes.data, batch) == 0
+    libf.cleanup(p)
+    assert rel_l2(y, ref) <= 2e-6
+    pi = libf.L.kfft_config_cpx(n, 1 | (1 << 8), None, None)
+    z = np.empty_like(x)
+    assert libf.L.kfft_eval_cpx_batch(pi, y.ctypes.data, z.ctypes.data, batch) == 0
+    libf.cleanup(pi)
+    assert rel_l2(z, x) <= 4e-6
