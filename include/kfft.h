@@ -37,6 +37,27 @@ extern "C" {
 #define KFFT_API __attribute__((visibility("default")))
 #endif
 
+/* ---- config.h.in:30-37: the 2D, convolution and 2D convolution extensions
+ * are always built into this library, so code that tests for them (the tiny
+ * API, kfft_tiny.h) sees them enabled. */
+#ifndef KFFT_2D_ENABLE
+#define KFFT_2D_ENABLE
+#endif
+#ifndef KFFT_CONV_ENABLE
+#define KFFT_CONV_ENABLE
+#endif
+#ifndef KFFT_CONV2D_ENABLE
+#define KFFT_CONV2D_ENABLE
+#endif
+
+/* ---- incs/kfft_macro.h:139-144 ------------------------------------------ */
+#define KFFT_UNUSED_VAR(X) (void)(X)
+#if defined(_MSC_VER)
+#define KFFT_UNUSED_FUNC
+#else
+#define KFFT_UNUSED_FUNC __attribute__((__unused__))
+#endif
+
 /* ---- incs/kfft_types.h:21-31 ------------------------------------------- */
 #if defined(KFFT_HALF_SCALAR)
 typedef float kfft_scalar;

@@ -282,6 +282,53 @@ def dft_exact(x, inverse: bool = False):
 
 
 # ---------------------------------------------------------------------------
+# post-transform helpers: fftshift and the kfft_math API (index arithmetic,
+# restated in numpy; no floating-point rounding beyond one operation each)
+# ---------------------------------------------------------------------------
+def shift(a, inverse: bool = False):
+    """fftshift (forward) / ifftshift (inverse) of every axis of a 1D or 2D array.
+
+    Follows kfft_shift.c:4-31 for one axis: an odd length n = 2c+1 moves
+    element (i + c + 1) mod n to i going forward and (i + c) mod n going
+    back; an even length swaps its halves both ways (the intent of
+    kfft_shift.c:10-11, whose swap macro zeroes the data in the reference
+    build).  2D arrays (sz_y rows of sz_x) are shifted along the rows, then
+    along the columns, as ext/2d/kfft_cpx2.c:188-226 does through transposes.
+    """
+    a = np.asarray(a)
+    out = a
+    for ax in range(a.ndim):
+        n = a.shape[ax]
+        c = n // 2
+        k = c if inverse else (n - c)
+        # new[i] = old[(i + k) mod n]
+        out = np.roll(out, -k, axis=ax)
+    return out
+
+
+def magnitude(z):
+    """|z| = sqrt(re^2 + im^2) per element in the working precision (kfft_math.h:153-155)."""
+    z = np.asarray(z)
+    r = z.real
+    i = z.imag
+    return np.sqrt(r * r + i * i)
+
+
+def average(v):
+    """Sum of the elements in index order, divided by the count (kfft_math.c:139-148)."""
+    v = np.asarray(v)
+    acc = v.dtype.type(0)
+    for e in v.tolist():
+        acc = v.dtype.type(acc + e)
+    return v.dtype.type(acc / v.dtype.type(len(v)))
+
+
+def transpose(a):
+    """Fout[i][j] = Fin[j][i] for Fin of y rows by x columns (kfft_math.c:60-78)."""
+    return np.ascontiguousarray(np.asarray(a).T)
+
+
+# ---------------------------------------------------------------------------
 # The reference library itself (present only where oracle/build_ref.sh ran).
 # ---------------------------------------------------------------------------
 def ref_library_path(precision: str = "double") -> str | None:
