@@ -87,6 +87,61 @@ KFFT_API kfft_return_t kfft_eval_cpx_noalloc(kfft_plan_cpx* plan, const kfft_cpx
 KFFT_API size_t kfft_noalloc_scratch_bytes(void);
 KFFT_API const char* kfft_noalloc_last_message(void);
 
+/*
+ * Plan variants and the tuning table.  The reference plans one way per length
+ * (kfft_generic.c:129-151 factorisation); the engine can split a length into
+ * passes several ways (largest pass length, lanes per tile, one fused pass or
+ * several, shared-memory or register tiles, tensor-core radix-16 stages) and
+ * lets a tuner choose.  Variant 0 is the built-in default; every variant
+ * computes the same transform (the tensor-core variant only in the float
+ * build and only for plans whose flags carry KFFT_FLAG_TENSOR_CORES, because
+ * it trades accuracy for speed).
+ *
+ * kfft_config_cpx_variant builds a complex plan with an explicit variant and
+ * otherwise behaves as kfft_config_cpx.  kfft_tune_set records that complex
+ * plans of length nfft with the direction and tensor-core bits of `flags`
+ * should use `variant`; every later kfft_config_cpx (and every complex plan a
+ * scalar, 2D or convolution plan builds inside) then uses it.  An explicit or
+ * tuned variant decides the tensor-core stages itself; without one,
+ * KFFT_FLAG_TENSOR_CORES alone does.  The table is process-wide and
+ * thread-safe.  kfft_tune_get returns the recorded variant or -1.
+ */
+KFFT_API uint32_t kfft_variant_count(void);
+KFFT_API kfft_plan_cpx* kfft_config_cpx_variant(uint32_t nfft, uint32_t flags, uint32_t variant,
+                                                kfft_pool_t* A, size_t* lenmem);
+KFFT_API kfft_return_t kfft_tune_set(uint32_t nfft, uint32_t flags, uint32_t variant);
+KFFT_API int kfft_tune_get(uint32_t nfft, uint32_t flags);
+KFFT_API void kfft_tune_clear(void);
+
+/*
+ * Cost model of the tuner: a 3-layer MLP (in_dim -> 64 -> 64 -> 1, ReLU) kept
+ * in device memory and trained by the engine's own CUDA kernels in FP32 with
+ * Adam on mean squared error.  Rows of X are feature vectors (row-major,
+ * n x in_dim, host memory, in_dim <= 64), y the targets.  The model only
+ * ranks plan variants; it never touches transform arithmetic.  No
+ * counterpart in the reference, whose planner has one fixed rule.
+ *   kfft_mlp_create    new model with seeded He-uniform weights, NULL on error
+ *   kfft_mlp_params    number of FP32 parameters (W1,b1,W2,b2,W3,b3 packed)
+ *   kfft_mlp_get/set   copy the packed parameters out of / into the model
+ *   kfft_mlp_predict   out[i] = f(X[i])
+ *   kfft_mlp_loss_grad loss = mean (f(X)-y)^2 and its gradient (packed like
+ *                      the parameters) over all n rows, without an update
+ *   kfft_mlp_train     `epochs` passes of minibatch Adam; returns the final
+ *                      full-set loss in *loss (may be NULL)
+ */
+typedef struct kfft_mlp kfft_mlp;
+KFFT_API kfft_mlp* kfft_mlp_create(uint32_t in_dim, uint64_t seed);
+KFFT_API void kfft_mlp_release(kfft_mlp* m);
+KFFT_API uint32_t kfft_mlp_params(const kfft_mlp* m);
+KFFT_API kfft_return_t kfft_mlp_get(const kfft_mlp* m, float* params);
+KFFT_API kfft_return_t kfft_mlp_set(kfft_mlp* m, const float* params);
+KFFT_API kfft_return_t kfft_mlp_predict(kfft_mlp* m, const float* X, uint32_t n, float* out);
+KFFT_API kfft_return_t kfft_mlp_loss_grad(kfft_mlp* m, const float* X, const float* y,
+                                          uint32_t n, float* loss, float* grad);
+KFFT_API kfft_return_t kfft_mlp_train(kfft_mlp* m, const float* X, const float* y, uint32_t n,
+                                      uint32_t epochs, uint32_t minibatch, float lr,
+                                      uint64_t seed, float* loss);
+
 /* Engine introspection (used by tests and the benchmark). */
 typedef struct {
     uint64_t kernel_launches; /* kernels this library launched since load */

@@ -22,6 +22,7 @@ FLAG_GENERIC = 1 << 2
 FLAG_GENERIC_ONLY = 1 << 3
 FLAG_EXPAND_SCALAR = 1 << 4
 FLAG_DISABLE_NORM = 1 << 5
+FLAG_TENSOR_CORES = 1 << 8
 
 RET_SUCCESS = 0
 RET_ALLOC_FAIL = 1
@@ -56,6 +57,10 @@ EXPORTED_SYMBOLS = [
     "kfft_math_hadamard_cpx", "kfft_math_hadamard_scalar", "kfft_math_transpose_cpx",
     "kfft_math_transpose_scalar", "kfft_math_transpose_ip_cpx", "kfft_math_transpose_ip_scalar",
     "kfft_math_magnitude", "kfft_math_magnitude_ip", "kfft_math_average",
+    "kfft_variant_count", "kfft_config_cpx_variant", "kfft_tune_set", "kfft_tune_get",
+    "kfft_tune_clear",
+    "kfft_mlp_create", "kfft_mlp_release", "kfft_mlp_params", "kfft_mlp_get", "kfft_mlp_set",
+    "kfft_mlp_predict", "kfft_mlp_loss_grad", "kfft_mlp_train",
 ]
 
 
@@ -167,6 +172,29 @@ class KfftLib:
         L.kfft_math_magnitude_ip.argtypes = [vp, u32]
         L.kfft_math_average.argtypes = [vp, u32]
         L.kfft_math_average.restype = ctypes.c_float if precision == "float" else ctypes.c_double
+        L.kfft_variant_count.restype = u32
+        L.kfft_config_cpx_variant.restype = vp
+        L.kfft_config_cpx_variant.argtypes = [u32, u32, u32, vp, vp]
+        L.kfft_tune_set.restype = ctypes.c_uint
+        L.kfft_tune_set.argtypes = [u32, u32, u32]
+        L.kfft_tune_get.restype = ctypes.c_int
+        L.kfft_tune_get.argtypes = [u32, u32]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.kfft_mlp_create.restype = vp
+        L.kfft_mlp_create.argtypes = [u32, ctypes.c_uint64]
+        L.kfft_mlp_release.argtypes = [vp]
+        L.kfft_mlp_params.restype = u32
+        L.kfft_mlp_params.argtypes = [vp]
+        for n in ("kfft_mlp_get", "kfft_mlp_set"):
+            getattr(L, n).restype = ctypes.c_uint
+            getattr(L, n).argtypes = [vp, vp]
+        L.kfft_mlp_predict.restype = ctypes.c_uint
+        L.kfft_mlp_predict.argtypes = [vp, vp, u32, vp]
+        L.kfft_mlp_loss_grad.restype = ctypes.c_uint
+        L.kfft_mlp_loss_grad.argtypes = [vp, vp, vp, u32, fp, vp]
+        L.kfft_mlp_train.restype = ctypes.c_uint
+        L.kfft_mlp_train.argtypes = [vp, vp, vp, u32, u32, u32, ctypes.c_float, ctypes.c_uint64,
+                                     fp]
         L.kfft_gb300_last_error.restype = ctypes.c_char_p
         L.kfft_gb300_describe.restype = ctypes.c_char_p
         L.kfft_gb300_describe.argtypes = [vp]

@@ -23,7 +23,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 SOURCES = ["pass_smem.cu", "pass_reg.cu", "persistent.cu", "tables.cu", "plan.cu", "api.cu",
-           "uneven.cu", "noalloc.cu", "helpers.cu"]
+           "uneven.cu", "noalloc.cu", "helpers.cu", "mlp.cu"]
 HEADERS = ["engine.cuh", "fft_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libkfft_gb300.so": [], "libkfft_gb300_f.so": ["-DKFFT_HALF_SCALAR"]}

@@ -18,6 +18,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.cuh"
@@ -359,8 +360,32 @@ size_t cpx_memneed(uint32_t nfft) {
     return sizeof(kfft_plan_cpx) + (nfft ? gpu_handle_bytes() + 16 : 0);
 }
 
+// tuning table: (nfft, direction and tensor-core bits) -> plan variant
+constexpr uint32_t kTuneKeyFlags = KFFT_FLAG_INVERSE | KFFT_FLAG_TENSOR_CORES;
+std::mutex g_tune_mu;
+std::unordered_map<uint64_t, uint32_t> g_tune;
+
+uint64_t tune_key(uint32_t nfft, uint32_t flags) {
+    return (uint64_t(nfft) << 32) | (flags & kTuneKeyFlags);
+}
+
+// the variant a plan built without an explicit choice uses, -1 if none
+int tuned_variant(uint32_t nfft, uint32_t flags) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(nfft, flags));
+    return it == g_tune.end() ? -1 : int(it->second);
+}
+
+bool variant_allowed(uint32_t variant, uint32_t flags) {
+    if (variant >= kfft_variant_count()) return false;
+    // the tensor-core variant only where the caller accepts its accuracy
+    if (plan_variant(variant).tc && !(flags & KFFT_FLAG_TENSOR_CORES)) return false;
+    return true;
+}
+
 // builds the device side of a complex plan node allocated in pool mm
-bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm) {
+bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm,
+              int variant = -1) {
     P->nfft = nfft;
     P->flags = flags;
     P->level = 0;
@@ -370,10 +395,15 @@ bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm) 
     if (!g) return false;
     const int sign = (flags & KFFT_FLAG_INVERSE) ? +1 : -1;
     cudaStream_t st = sync_stream();
-    g->plan = make_plan(nfft, sign, *g->arena, st);
+    // an explicit or tuned variant fixes every knob, tensor cores included;
+    // otherwise the default split runs and the flag alone decides them
+    const int chosen = variant >= 0 ? variant : tuned_variant(nfft, flags);
+    uint32_t v = chosen >= 0 ? uint32_t(chosen) : 0u;
+    if (!variant_allowed(v, flags)) v = 0;
+    g->plan = make_plan(nfft, sign, *g->arena, st, kMaxDirectPrime, plan_variant(v));
     if (!g->plan) return false;
 #if defined(KFFT_HALF_SCALAR)
-    set_tensor_cores(g->plan, (flags & KFFT_FLAG_TENSOR_CORES) != 0);
+    if (chosen < 0) set_tensor_cores(g->plan, (flags & KFFT_FLAG_TENSOR_CORES) != 0);
 #endif
     if (finish(st) != KFFT_RET_SUCCESS) return false;
     P->gpu = g;
@@ -409,6 +439,45 @@ KFFT_API kfft_plan_cpx* kfft_config_cpx(const uint32_t nfft, const uint32_t flag
         return NULL;
     }
     return P;
+}
+
+KFFT_API uint32_t kfft_variant_count(void) {
+#if defined(KFFT_HALF_SCALAR)
+    return kPlanVariants;
+#else
+    return kPlanVariants - 1;  // no tensor-core variant in the double build
+#endif
+}
+
+KFFT_API kfft_plan_cpx* kfft_config_cpx_variant(uint32_t nfft, uint32_t flags, uint32_t variant,
+                                                kfft_pool_t* A, size_t* lenmem) {
+    if (!variant_allowed(variant, flags)) return NULL;
+    kfft_pool_t* mm = nullptr;
+    kfft_plan_cpx* P = plan_prepare<kfft_plan_cpx>(flags, cpx_memneed(nfft), A, lenmem, &mm);
+    if (!P) return NULL;
+    if (!cpx_init(P, nfft, flags, mm, int(variant))) {
+        plan_terminate(P, A);
+        return NULL;
+    }
+    return P;
+}
+
+KFFT_API kfft_return_t kfft_tune_set(uint32_t nfft, uint32_t flags, uint32_t variant) {
+    if (nfft == 0 || !variant_allowed(variant, flags)) return KFFT_RET_BADARGUMENTS;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_key(nfft, flags)] = variant;
+    return KFFT_RET_SUCCESS;
+}
+
+KFFT_API int kfft_tune_get(uint32_t nfft, uint32_t flags) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(nfft, flags));
+    return it == g_tune.end() ? -1 : int(it->second);
+}
+
+KFFT_API void kfft_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
 }
 
 KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* fin,

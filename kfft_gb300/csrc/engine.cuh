@@ -169,8 +169,20 @@ struct PassSpec {
 
 struct DeviceArena;  // device memory owned by a plan tree
 
+// Planner knobs one plan variant fixes (the tuner's search space).
+struct PlanVariant {
+    uint32_t rmax = 1024;        // largest pass length of a multi-pass split
+    uint32_t lanes = 0;          // lanes of multi-pass tiles (0: precision default)
+    uint32_t single_cap = 4096;  // longest length run as one fused pass
+    bool no_fused = false;       // shared-memory ping-pong tiles only
+    bool tc = false;             // radix-16 stages on tensor cores (FP32 build)
+};
+constexpr uint32_t kPlanVariants = 6;
+PlanVariant plan_variant(uint32_t index);
+
 struct FftPlan {
     uint32_t N = 0;
+    PlanVariant var;
     int sign = -1;  // -1 forward, +1 inverse
     bool tc = false;  // radix-16 passes on tensor cores (FP32 build)
     Method method = METHOD_DIRECT;
@@ -217,7 +229,7 @@ struct DeviceArena {
 // Builds the plan of an N-point transform of direction `sign` on the current
 // device, allocating its tables from `arena`.  Returns nullptr on failure.
 FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
-                   uint32_t max_prime = kMaxDirectPrime);
+                   uint32_t max_prime = kMaxDirectPrime, const PlanVariant& var = PlanVariant());
 bool is_direct_length(uint32_t n, uint32_t max_prime = kMaxDirectPrime);
 // Marks a plan tree to run its radix-16 passes on tensor cores (FP32 build).
 void set_tensor_cores(FftPlan* p, bool on);

@@ -226,10 +226,13 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     // tiles of kRegLanes lanes fit); others use the shared-memory ping-pong tile
     bool small_radices = true;
     for (uint32_t f : prime_factors(N)) small_radices = small_radices && f <= 13;
-    if (small_radices && reg_tile_fits(N, 1)) {
+    const PlanVariant& V = P->var;
+    if (V.no_fused) small_radices = false;
+    if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1)) {
         Rs.push_back(N);
     } else if (small_radices) {
         for (uint32_t rmax : {1024u, 768u, 512u, 384u, 256u, 128u, 64u, 32u, 16u}) {
+            if (rmax > V.rmax) continue;
             std::vector<uint32_t> cand = split_passes(N, rmax);
             bool ok = !cand.empty();
             for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R));
@@ -240,8 +243,8 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
         }
     }
     if (Rs.empty()) {
-        if (N <= tile_capacity()) Rs.push_back(N);
-        else Rs = split_passes(N, kMultiRmax);
+        if (N <= tile_capacity() && N <= std::max(V.single_cap, kRegTile)) Rs.push_back(N);
+        else Rs = split_passes(N, std::min(kMultiRmax, V.rmax));
     }
     if (Rs.empty()) return false;
     std::map<uint32_t, const vec2_t*> inner;
@@ -310,10 +313,27 @@ static bool transform_once(const FftPlan& plan, const vec2_t* in, vec2_t* out, c
     return ok;
 }
 
+PlanVariant plan_variant(uint32_t index) {
+    PlanVariant v;
+    switch (index) {
+        case 1: v.rmax = 512; break;
+        case 2: v.rmax = 256; v.lanes = 16; break;
+        case 3: v.no_fused = true; break;
+        case 4: v.single_cap = 1024; break;
+        case 5: v.tc = true; break;
+        default: break;
+    }
+    return v;
+}
+
 FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
-                   uint32_t max_prime) {
+                   uint32_t max_prime, const PlanVariant& var) {
     FftPlan* P = new FftPlan();
     P->N = N;
+    P->var = var;
+#if defined(KFFT_HALF_SCALAR)
+    P->tc = var.tc;
+#endif
     P->sign = sign;
     if (N == 0) return P;
     if (is_direct_length(N, max_prime)) {
@@ -352,8 +372,8 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
         cudaMemcpyAsync(dip, ip.data(), sizeof(uint32_t) * L, cudaMemcpyHostToDevice, st);
         P->gperm = dgp;
         P->iperm = dip;
-        P->sub_fwd = make_plan(L, -1, arena, st, max_prime);
-        P->sub_inv = make_plan(L, +1, arena, st, max_prime);
+        P->sub_fwd = make_plan(L, -1, arena, st, max_prime, var);
+        P->sub_inv = make_plan(L, +1, arena, st, max_prime, var);
         if (!P->sub_fwd || !P->sub_inv) {
             delete P;
             return nullptr;
@@ -385,8 +405,8 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
     }
     gen_chirp(chirp, N, N, sign, st);
     gen_bluestein_filter(filt, chirp, N, uint32_t(M), st);
-    P->sub_fwd = make_plan(uint32_t(M), -1, arena, st, max_prime);
-    P->sub_inv = make_plan(uint32_t(M), +1, arena, st, max_prime);
+    P->sub_fwd = make_plan(uint32_t(M), -1, arena, st, max_prime, var);
+    P->sub_inv = make_plan(uint32_t(M), +1, arena, st, max_prime, var);
     if (!P->sub_fwd || !P->sub_inv) {
         delete P;
         return nullptr;
@@ -416,10 +436,18 @@ std::string describe(const FftPlan& p) {
         o << " L=" << p.L << " [" << describe(*p.sub_fwd) << "]";
         return o.str();
     }
+    bool has16 = false;
     for (const PassSpec& s : p.passes) {
         o << " | R=" << s.R << " Ns=" << s.Ns << " radices=";
-        for (size_t i = 0; i < s.radices.size(); ++i) o << (i ? "," : "") << int(s.radices[i]);
+        for (size_t i = 0; i < s.radices.size(); ++i) {
+            o << (i ? "," : "") << int(s.radices[i]);
+            has16 = has16 || s.radices[i] == 16;
+        }
     }
+    // variant knobs that change the kernels but not the pass split
+    if (p.var.lanes && p.passes.size() > 1) o << " | lanes=" << p.var.lanes;
+    if (p.var.no_fused) o << " | smem";
+    if (p.tc && has16) o << " | tc";
     return o.str();
 }
 
@@ -492,7 +520,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.load_mode = MODE_ELEM;
         d.store_mode = MODE_ELEM;
     } else {
-        C = std::min(kMultiLanes, d.lanes_j);
+        C = std::min(P.var.lanes ? P.var.lanes : kMultiLanes, d.lanes_j);
         d.load_mode = MODE_LANE;
         d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
     }
@@ -500,7 +528,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     // register-resident tile when every inner radix is <= 16 and each thread's
     // share of every inner pass fits its register budget (lower C if needed)
     {
-        bool radix_ok = !s.radices.empty() || s.R == 1;
+        bool radix_ok = (!s.radices.empty() || s.R == 1) && !P.var.no_fused;
         for (uint8_t r : s.radices) radix_ok = radix_ok && r <= 16;
         for (uint32_t c = C; radix_ok && c >= 1; --c) {
             const bool fits = reg_tile_fits(s.R, c);
@@ -514,6 +542,8 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
             if (!coalesced_enough) break;
         }
     }
+    // a shared-memory tile must fit the per-CTA budget whatever the variant asked
+    while (!d.regmode && C > 1 && smem_for(C * s.R) > kSmemBudget) --C;
     d.C = C;
     const uint64_t lanes = uint64_t(d.batch) * d.lanes_j;
     d.tiles = uint32_t((lanes + C - 1) / C);
