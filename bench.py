@@ -1,7 +1,7 @@
 """Benchmark of the GB300 FFT engine (one JSON line on rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload uneven|c2c4096]
+                    [--workload uneven|learned_planner|c2c4096|...]
 
 Metric: 5*N*log2(N) GFLOP/s summed over every transform of a step (forward and
 inverse counted separately), the reference's own throughput convention
@@ -417,6 +417,65 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_learned_planner(args):
+    """Learned-planner sweep: complex fp32 lengths N = 1, 102, 203, ... <= 10^6
+    (every `--stride`-th of them), batch ceil(2^24 / N).  Every plan variant of
+    every length is timed (the exhaustive tuner); the MLP cost model is trained
+    on the timings of 20% of the lengths (chosen by seed) with the engine's own
+    CUDA kernels and proposes a variant for each of the other lengths.  The
+    line reports the throughput of the proposed plans, of the plain (default)
+    plans and of the best measured plans on those lengths, and the regret."""
+    import torch
+    import kfft_gb300
+    from kfft_gb300 import tuner as T
+
+    torch.cuda.set_device(0)
+    lib = kfft_gb300.load("float")
+    lengths = list(range(1, 1_000_001, 101))[::max(1, args.stride)]
+    t0 = time.perf_counter()
+    recs = T.exhaustive(lib, lengths, points=1 << 24, reps=max(3, args.steps),
+                        warmup=args.warmup)
+    sweep_s = time.perf_counter() - t0
+    train, test = T.split_lengths(recs, 0.2, seed=7)
+    model = T.CostModel(lib, seed=3)
+    t1 = time.perf_counter()
+    loss = model.fit(train, epochs=300)
+    train_s = time.perf_counter() - t1
+    r = T.evaluate(model, test)
+    if args.tune_db:
+        db = T.TuneDB(args.tune_db)
+        db.update("float", recs)
+        db.save()
+        model.save(args.tune_db + ".model.npz")
+    model.close()
+    n_test = r.lengths
+    peak, peak_kind = measured_peaks()
+    g = T.by_length(test)
+    bytes_total = sum(2 * 8 * n * next(iter(v.values())).batch for n, v in g.items())
+    achieved = bytes_total / (r.ms_chosen / 1e3) / 1e9
+    line = {"metric": "5N*log2N GFLOP/s", "value": round(r.gflops_chosen, 2), "unit": "GFLOP/s",
+            "n_gpus": 1, "steps": n_test, "warmup": args.warmup,
+            "ms_per_step": round(r.ms_chosen / max(n_test, 1), 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"learned planner: complex fp32 N = 1 + 101 k <= 10^6, every "
+                                   f"{max(1, args.stride)}-th ({len(lengths)} lengths), batch "
+                                   f"ceil(2^24/N), one forward transform per length",
+                       "l2": "2^24-point launches (128 MB) rotate through one buffer"},
+            "learned_planner": {
+                "lengths_train": len({x.n for x in train}), "lengths_test": n_test,
+                "records": len(recs), "variants": lib.L.kfft_variant_count(),
+                "regret_geomean": round(r.geomean_regret, 4), "regret_max": round(r.max_regret, 4),
+                "hit_rate": round(r.hit_rate, 4), "gain_vs_plain_geomean": round(r.geomean_gain, 4),
+                "gflops_plain": round(r.gflops_default, 2), "gflops_best": round(r.gflops_best, 2),
+                "gflops_chosen": round(r.gflops_chosen, 2), "train_loss": round(loss, 5),
+                "sweep_s": round(sweep_s, 1), "train_s": round(train_s, 2),
+                "worst": [[round(a, 3), int(b), int(c)] for a, b, c in r.worst]},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "peak_source": peak_kind, "kernel": "k_pass_reg / k_pass (proposed plans)"}}
+    print(json.dumps(line), flush=True)
+
+
 def make_workload(name, lib, need_lib=True, subset=1, precision="float"):
     if name in UNIFORM_WORKLOADS:
         return UNIFORM_WORKLOADS[name](lib)
@@ -430,7 +489,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("KFFT_BENCH_WORKLOAD", "uneven"),
-                    choices=["uneven"] + sorted(UNIFORM_WORKLOADS))
+                    choices=["uneven", "learned_planner"] + sorted(UNIFORM_WORKLOADS))
+    ap.add_argument("--stride", type=int, default=1,
+                    help="learned_planner: keep every k-th length of the sweep")
+    ap.add_argument("--tune-db", default="",
+                    help="learned_planner: write the tuning table (JSON) and model here")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--subset", type=int, default=1,
                     help="profiling only: keep every k-th sequence of the uneven batch")
@@ -441,6 +504,10 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.workload == "learned_planner":
+        if rank == 0:
+            run_learned_planner(args)
         return
 
     import torch
@@ -550,7 +617,7 @@ def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind):
         achieved = total_bytes / (ms_step / 1e3) / 1e9
         return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None,
-                "peak_source": peak_kind, "kernel": "k_pass (all passes of the batch)"}
+                "peak_source": peak_kind, "kernel": "k_persistent (all passes of the batch)"}
     dur = ms_step / n
     achieved = per / (dur / 1e3) / 1e9
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
