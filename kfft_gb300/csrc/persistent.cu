@@ -12,8 +12,6 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_item;
     __shared__ uint32_t s_ok;
-    __shared__ __align__(16) PassDesc s_desc;
-    __shared__ __align__(16) PassExtra s_extra;
     vec2_t* buf = reinterpret_cast<vec2_t*>(smem_raw);
     while (true) {
         if (threadIdx.x == 0) s_item = atomicAdd(head, 1u);
@@ -28,19 +26,15 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
             if (!ok) atomicExch(error, 1u);
             s_ok = ok ? 1u : 0u;
         }
-        // stage the descriptor in shared memory
-        {
-            const uint32_t* src = reinterpret_cast<const uint32_t*>(&descs[q.desc]);
-            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_desc);
-            for (uint32_t i = threadIdx.x; i < sizeof(PassDesc) / 4; i += blockDim.x) dst[i] = src[i];
-            const uint32_t* xs = reinterpret_cast<const uint32_t*>(&extras[q.desc]);
-            uint32_t* xd = reinterpret_cast<uint32_t*>(&s_extra);
-            for (uint32_t i = threadIdx.x; i < sizeof(PassExtra) / 4; i += blockDim.x) xd[i] = xs[i];
-        }
         __syncthreads();
         if (s_ok) {
-            if (s_desc.inv) tile_body_reg<true>(s_desc, s_extra, q.tile, buf);
-            else tile_body_reg<false>(s_desc, s_extra, q.tile, buf);
+            // descriptor and inner steps are read where they lie (read-only,
+            // cached): no copy into shared memory, which the tile buffers'
+            // stores would force the compiler to reload after every store
+            const PassDesc& d = descs[q.desc];
+            const PassExtra& x = extras[q.desc];
+            if (d.inv) tile_body_reg<true>(d, x, q.tile, buf);
+            else tile_body_reg<false>(d, x, q.tile, buf);
         }
         __threadfence();
         __syncthreads();

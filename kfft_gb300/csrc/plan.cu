@@ -181,6 +181,37 @@ static std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
     return {};
 }
 
+// Length of the Bluestein convolution for a minimum of m: the 7-smooth M >= m
+// (up to 2m) with the least estimated cost M * passes(M) * (1 + 0.15 * odd
+// factors).  A pass is one HBM round trip, and radix-3/5/7 stages cost about
+// 30% more per point than radix-2/4/8/16 ones on this kernel; the nearest
+// 7-smooth length is often odd-heavy or one pass deeper than a power-of-two
+// one slightly above it.
+static uint64_t bluestein_length(uint64_t m) {
+    uint64_t best = next_smooth(m);
+    double best_cost = -1.0;
+    for (uint64_t a = 1; a <= 2 * m; a *= 2)
+        for (uint64_t b = a; b <= 2 * m; b *= 3)
+            for (uint64_t c = b; c <= 2 * m; c *= 5)
+                for (uint64_t d = c; d <= 2 * m; d *= 7) {
+                    if (d < m || d > 0xFFFFFFFFull) continue;
+                    uint64_t r = d;
+                    int odd = 0;
+                    for (uint64_t q : {3ull, 5ull, 7ull})
+                        while (r % q == 0) {
+                            r /= q;
+                            ++odd;
+                        }
+                    const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), kMultiRmax).size());
+                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) * (1.0 + 0.15 * odd);
+                    if (best_cost < 0 || cost < best_cost) {
+                        best_cost = cost;
+                        best = d;
+                    }
+                }
+    return best;
+}
+
 // ---------------------------------------------------------------------------
 // device arena
 // ---------------------------------------------------------------------------
@@ -390,7 +421,7 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
     }
     // ---- Bluestein: X_k = c_k sum_n (x_n c_n) conj(c_{k-n}) --------------------
     P->method = METHOD_BLUESTEIN;
-    uint64_t M = next_smooth(2 * uint64_t(N) - 1);
+    uint64_t M = bluestein_length(2 * uint64_t(N) - 1);
     if (M > 0xFFFFFFFFull) {
         delete P;
         return nullptr;
@@ -520,7 +551,12 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.load_mode = MODE_ELEM;
         d.store_mode = MODE_ELEM;
     } else {
-        C = std::min(P.var.lanes ? P.var.lanes : kMultiLanes, d.lanes_j);
+        // enough lanes that every thread has a butterfly in every inner stage
+        // (C * R / radix >= threads), at least kMultiLanes for row segments
+        uint32_t want = kMultiLanes;
+        for (uint8_t r : s.radices)
+            want = std::max<uint32_t>(want, (kPassThreads * r + s.R - 1) / s.R);
+        C = std::min(P.var.lanes ? P.var.lanes : want, d.lanes_j);
         d.load_mode = MODE_LANE;
         d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
     }
