@@ -24,12 +24,22 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
     return uint32_t((uint64_t(__umulhi(n, f.m)) + n) >> f.s);
 }
 
+#if defined(KFFT_HALF_SCALAR)
+// FP32: Blackwell's paired FP32 instructions work on a float2 at once (one
+// instruction for both parts, each rounded as the scalar operation would be)
+__device__ __forceinline__ vec2_t cadd(vec2_t a, vec2_t b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ vec2_t csub(vec2_t a, vec2_t b) {
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);  // a - b, one rounding
+}
+__device__ __forceinline__ vec2_t cscale(vec2_t a, real_t s) { return __fmul2_rn(a, make_float2(s, s)); }
+#else
 __device__ __forceinline__ vec2_t cadd(vec2_t a, vec2_t b) { return {a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ vec2_t csub(vec2_t a, vec2_t b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ vec2_t cscale(vec2_t a, real_t s) { return {a.x * s, a.y * s}; }
+#endif
 __device__ __forceinline__ vec2_t cmul(vec2_t a, vec2_t b) {
     return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 }
-__device__ __forceinline__ vec2_t cscale(vec2_t a, real_t s) { return {a.x * s, a.y * s}; }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
 __device__ __forceinline__ vec2_t rot(vec2_t a) {
@@ -566,12 +576,10 @@ __device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint3
                 v[q] = __ldcg(&d.in[base + uint64_t(__ldg(&d.pro_perm[n])) * d.in_es]);
             }
             break;
-        default: {
-            const vec2_t* p0 = d.in + (base + first);
+        default:
 #pragma unroll
-            for (int q = 0; q < P; ++q) v[q] = __ldcg(p0 + q * step);
+            for (int q = 0; q < P; ++q) v[q] = __ldcg(&d.in[base + first + q * step]);
             break;
-        }
     }
     if (d.Ns > 1) {
         const uint32_t kq = fdiv(j, d.div_Ns);
@@ -628,11 +636,10 @@ __device__ __forceinline__ void fused_store(const PassDesc& d, uint32_t bs, uint
     const uint32_t ko = j - blo * d.Ns;
     const uint32_t base = blo * d.Ns * d.R + ko;
     if (d.epi_op == EPI_NONE) {
+        vec2_t* o = d.out + uint64_t(bs) * d.out_bs;
         const uint64_t es = d.out_es;
-        vec2_t* o = d.out + uint64_t(bs) * d.out_bs + uint64_t(base + ob * d.Ns) * es;
-        const uint64_t step = uint64_t(ns) * d.Ns * es;
 #pragma unroll
-        for (int q = 0; q < P; ++q) o[q * step] = cscale(v[q], d.scale);
+        for (int q = 0; q < P; ++q) o[uint64_t(base + (ob + q * ns) * d.Ns) * es] = cscale(v[q], d.scale);
     } else {
 #pragma unroll
         for (int q = 0; q < P; ++q) store_elem(d, bs, base + (ob + q * ns) * d.Ns, v[q]);
@@ -651,16 +658,6 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
     const uint32_t items = d.C * m;
     const bool cfast = (sio == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
                                           : ((dio == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
-    // pad() adds one slot per kPad elements, so pad(x + q s) is linear in q
-    // when s is a multiple of kPad, or when s == 1 and the P elements stay
-    // inside one period (P divides kPad and x is a multiple of P): then the P
-    // shared-memory addresses are one base plus q times a constant stride
-    constexpr uint32_t kPad = 1u << kPadShift;
-    const bool lin_ld = (m & (kPad - 1u)) == 0;
-    const uint32_t ld_stride = m + (m >> kPadShift);
-    const bool lin_st = ((st.ns & (kPad - 1u)) == 0) ||
-                        (st.ns == 1 && (kPad % P) == 0 && (d.R & (kPad - 1u)) == 0);
-    const uint32_t st_stride = st.ns + (st.ns >> kPadShift);
     for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
         uint32_t c, jj;
         if (cfast) {
@@ -690,10 +687,6 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
 #pragma unroll
                 for (int q = 0; q < P; ++q) v[q] = {real_t(0), real_t(0)};
             }
-        } else if (lin_ld) {
-            const vec2_t* p0 = src + pad(c * d.R + jj);
-#pragma unroll
-            for (int q = 0; q < P; ++q) v[q] = p0[q * ld_stride];
         } else {
 #pragma unroll
             for (int q = 0; q < P; ++q) v[q] = src[pad(c * d.R + jj + q * m)];
@@ -704,14 +697,8 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         dft<P, INV>(v);
         const uint32_t ob = blk * st.ns * P + kk;
         if (dio == IO_SMEM) {
-            if (lin_st) {
-                vec2_t* p0 = dst + pad(c * d.R + ob);
 #pragma unroll
-                for (int q = 0; q < P; ++q) p0[q * st_stride] = v[q];
-            } else {
-#pragma unroll
-                for (int q = 0; q < P; ++q) dst[pad(c * d.R + ob + q * st.ns)] = v[q];
-            }
+            for (int q = 0; q < P; ++q) dst[pad(c * d.R + ob + q * st.ns)] = v[q];
         } else if (live) {
             fused_store<P>(d, bs, j, ob, st.ns, v);
         }

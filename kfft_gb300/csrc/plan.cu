@@ -551,14 +551,14 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.load_mode = MODE_ELEM;
         d.store_mode = MODE_ELEM;
     } else {
-        // enough lanes that at least half the threads have a butterfly in
-        // every inner stage (C * R / radix >= threads / 2), and at least
-        // kMultiLanes for row segments.  Short passes (R <= 128) gain from the
-        // wider tiles; for R = 256 a full butterfly per thread measured slower
-        // than half of them idle.
+        // enough lanes that every thread has a butterfly in every inner stage
+        // (C * R / radix >= threads) for passes up to 128 points, half the
+        // threads from 256 points up (measured faster there than a full
+        // tile), and at least kMultiLanes for row segments
         uint32_t want = kMultiLanes;
+        const uint32_t share = s.R >= 256 ? 2u : 1u;
         for (uint8_t r : s.radices)
-            want = std::max<uint32_t>(want, (kPassThreads * r + 2 * s.R - 1) / (2 * s.R));
+            want = std::max<uint32_t>(want, (kPassThreads * r + share * s.R - 1) / (share * s.R));
         C = std::min(P.var.lanes ? P.var.lanes : want, d.lanes_j);
         d.load_mode = MODE_LANE;
         d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
