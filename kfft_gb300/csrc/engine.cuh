@@ -88,6 +88,7 @@ struct PassDesc {
     uint8_t tc;              // radix-16 inner passes on tensor cores (FP32 build)
     uint8_t nrad;
     uint8_t rad[kMaxInnerRadices];
+    uint8_t spec;            // log2 R of a compile-time power-of-two tile body, 0: generic
     FastDiv div_R, div_lanes_j, div_batch, div_Ns, div_C;
     const vec2_t* tw_inner;  // W_R^i, i < R
     const vec2_t* tw_lo;     // W_N^i, i < 2^tw_shift

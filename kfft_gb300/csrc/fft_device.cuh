@@ -906,6 +906,116 @@ __device__ __forceinline__ void tc_pass16(const PassDesc& d, const InnerStep& st
 }
 #endif
 
+// ---------------------------------------------------------------------------
+// compile-time tile bodies for power-of-two pass lengths R = 16..4096 (inner
+// radices 16,...,16 then 8, 4 or 2).  The same stages as fused_pass, with
+// every per-stage constant (butterflies per lane M = R/P, the stride NS of
+// the previous radices, the inner twiddle stride) known to the compiler: the
+// lane/butterfly split is a shift and a mask, and where padding keeps the P
+// shared-memory addresses of a butterfly equally spaced (a stride that is a
+// multiple of the pad period, or a unit stride inside one period) they are
+// one base plus immediate offsets.
+// ---------------------------------------------------------------------------
+template <int P, uint32_t R, uint32_t NS, int SIO, int DIO, bool INV>
+__device__ __forceinline__ void spec_stage(const PassDesc& d, const vec2_t* __restrict__ src,
+                                           vec2_t* __restrict__ dst, uint32_t lane0,
+                                           uint32_t total) {
+    constexpr uint32_t M = R / P;
+    constexpr uint32_t TWS = R / (NS * P);
+    constexpr uint32_t kPad = 1u << kPadShift;
+    constexpr bool kLinLd = (M % kPad) == 0;
+    constexpr bool kLinSt = (NS % kPad) == 0 || (NS == 1 && (kPad % P) == 0 && (R % kPad) == 0);
+    constexpr uint32_t kLdStride = M + (M >> kPadShift);
+    constexpr uint32_t kStStride = NS + (NS >> kPadShift);
+    const uint32_t items = d.C * M;
+    const bool cfast = (SIO == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
+                                          : ((DIO == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
+    for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
+        uint32_t c, jj;
+        if (cfast) {
+            jj = fdiv(it, d.div_C);
+            c = it - jj * d.C;
+        } else {
+            c = it / M;
+            jj = it % M;
+        }
+        const uint32_t g = lane0 + c;
+        uint32_t bs = 0, j = 0;
+        const bool live = g < total;
+        if ((SIO == IO_GLOBAL || DIO == IO_GLOBAL) && live) {
+            if (d.order == ORDER_J) {
+                bs = fdiv(g, d.div_lanes_j);
+                j = g - bs * d.lanes_j;
+            } else {
+                j = fdiv(g, d.div_batch);
+                bs = g - j * d.batch;
+            }
+        }
+        vec2_t v[P];
+        if constexpr (SIO == IO_GLOBAL) {
+            if (live) {
+                fused_load<P>(d, bs, j, jj, M, v);
+            } else {
+#pragma unroll
+                for (int q = 0; q < P; ++q) v[q] = {real_t(0), real_t(0)};
+            }
+        } else if constexpr (kLinLd) {
+            const vec2_t* p0 = src + pad(c * R + jj);
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[q] = p0[q * kLdStride];
+        } else {
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[q] = src[pad(c * R + jj + q * M)];
+        }
+        const uint32_t blk = jj / NS;
+        const uint32_t kk = jj % NS;
+        if constexpr (NS > 1) apply_inner_twiddles<P>(v, d.tw_inner, kk * TWS);
+        dft<P, INV>(v);
+        const uint32_t ob = blk * NS * P + kk;
+        if constexpr (DIO == IO_SMEM) {
+            if constexpr (kLinSt) {
+                vec2_t* p0 = dst + pad(c * R + ob);
+#pragma unroll
+                for (int q = 0; q < P; ++q) p0[q * kStStride] = v[q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < P; ++q) dst[pad(c * R + ob + q * NS)] = v[q];
+            }
+        } else if (live) {
+            fused_store<P>(d, bs, j, ob, NS, v);
+        }
+    }
+}
+
+constexpr uint32_t ilog2(uint32_t v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+
+// R = 16^K16 * T (T in 1, 2, 4, 8): stages of radix 16, then T; the same
+// ping-pong buffers as the generic body (A after stage 0, B after stage 1)
+template <uint32_t R, bool INV>
+__device__ __forceinline__ void tile_body_spec(const PassDesc& d, uint32_t lane0, uint32_t total,
+                                               vec2_t* bufA, vec2_t* bufB) {
+    constexpr uint32_t L = ilog2(R);
+    static_assert((1u << L) == R && L >= 4 && L <= 12, "power-of-two tile from 16 to 4096");
+    constexpr uint32_t K16 = L / 4;
+    constexpr int T = 1 << (L % 4);
+    constexpr int NP = int(K16) + (T > 1 ? 1 : 0);
+    constexpr int PL = T > 1 ? T : 16;  // radix of the last stage
+    if constexpr (NP == 1) {
+        spec_stage<16, R, 1, IO_GLOBAL, IO_GLOBAL, INV>(d, nullptr, nullptr, lane0, total);
+    } else if constexpr (NP == 2) {
+        spec_stage<16, R, 1, IO_GLOBAL, IO_SMEM, INV>(d, nullptr, bufA, lane0, total);
+        __syncthreads();
+        spec_stage<PL, R, 16, IO_SMEM, IO_GLOBAL, INV>(d, bufA, nullptr, lane0, total);
+    } else {
+        static_assert(NP == 3, "at most three inner stages");
+        spec_stage<16, R, 1, IO_GLOBAL, IO_SMEM, INV>(d, nullptr, bufA, lane0, total);
+        __syncthreads();
+        spec_stage<16, R, 16, IO_SMEM, IO_SMEM, INV>(d, bufA, bufB, lane0, total);
+        __syncthreads();
+        spec_stage<PL, R, 256, IO_SMEM, IO_GLOBAL, INV>(d, bufB, nullptr, lane0, total);
+    }
+}
+
 template <bool INV>
 __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
                                                const vec2_t* src, vec2_t* dst, uint32_t lane0,
@@ -952,6 +1062,18 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     }
     vec2_t* bufA = sm;
     vec2_t* bufB = sm + pad(d.C * d.R) + 1;
+    switch (d.spec) {
+        case 4: tile_body_spec<16, INV>(d, lane0, total, bufA, bufB); return;
+        case 5: tile_body_spec<32, INV>(d, lane0, total, bufA, bufB); return;
+        case 6: tile_body_spec<64, INV>(d, lane0, total, bufA, bufB); return;
+        case 7: tile_body_spec<128, INV>(d, lane0, total, bufA, bufB); return;
+        case 8: tile_body_spec<256, INV>(d, lane0, total, bufA, bufB); return;
+        case 9: tile_body_spec<512, INV>(d, lane0, total, bufA, bufB); return;
+        case 10: tile_body_spec<1024, INV>(d, lane0, total, bufA, bufB); return;
+        case 11: tile_body_spec<2048, INV>(d, lane0, total, bufA, bufB); return;
+        case 12: tile_body_spec<4096, INV>(d, lane0, total, bufA, bufB); return;
+        default: break;
+    }
     const vec2_t* src = nullptr;
 #if defined(KFFT_HALF_SCALAR)
     TcFrag Fr, Fi, Gm;

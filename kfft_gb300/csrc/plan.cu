@@ -584,6 +584,13 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     // a shared-memory tile must fit the per-CTA budget whatever the variant asked
     while (!d.regmode && C > 1 && smem_for(C * s.R) > kSmemBudget) --C;
     d.C = C;
+    // power-of-two register tiles of 16..4096 points run a compile-time body
+    d.spec = 0;
+    if (d.regmode && !d.tc && s.R >= 16 && s.R <= 4096 && (s.R & (s.R - 1)) == 0) {
+        uint32_t l = 0;
+        while ((1u << l) < s.R) ++l;
+        d.spec = uint8_t(l);
+    }
     const uint64_t lanes = uint64_t(d.batch) * d.lanes_j;
     d.tiles = uint32_t((lanes + C - 1) / C);
     uint32_t elems = C * s.R;
