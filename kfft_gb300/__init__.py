@@ -80,7 +80,8 @@ class InfoT(ctypes.Structure):
 
 
 def library_path(precision: str = "double") -> str:
-    return os.path.join(LIB_DIR, LIB_NAMES[precision])
+    """Path of one precision build; KFFT_GB300_LIB_DIR overrides the folder."""
+    return os.path.join(os.environ.get("KFFT_GB300_LIB_DIR") or LIB_DIR, LIB_NAMES[precision])
 
 
 def _ptr(a):

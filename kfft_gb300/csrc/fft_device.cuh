@@ -551,12 +551,11 @@ __device__ __forceinline__ void apply_inner_twiddles(vec2_t* v, const vec2_t* __
     for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&tw[q * step]));
 }
 
-// Loads the P inputs of one butterfly of the first inner pass straight from
-// global memory: prologue, then the outer twiddle W_{Ns*R}^{r*k} (applied in
-// groups of four to bound the registers held by table loads).
+// The P inputs of one butterfly of the first inner pass, straight from global
+// memory, through the prologue (chirp product or gather, if any).
 template <int P>
-__device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint32_t j, uint32_t jj,
-                                           uint32_t m, vec2_t* v) {
+__device__ __forceinline__ void prologue_load(const PassDesc& d, uint32_t bs, uint32_t j,
+                                              uint32_t jj, uint32_t m, vec2_t* v) {
     const uint64_t base = uint64_t(bs) * d.in_bs;
     const uint64_t step = uint64_t(m) * d.lanes_j * d.in_es;
     const uint64_t first = uint64_t(j + jj * d.lanes_j) * d.in_es;
@@ -581,6 +580,13 @@ __device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint3
             for (int q = 0; q < P; ++q) v[q] = __ldcg(&d.in[base + first + q * step]);
             break;
     }
+}
+
+// The outer twiddle W_{Ns*R}^{r*k} of the first inner pass (applied in groups
+// of four in FP64 to bound the registers held by table loads).
+template <int P>
+__device__ __forceinline__ void outer_twiddle(const PassDesc& d, uint32_t j, uint32_t jj,
+                                              uint32_t m, vec2_t* v) {
     if (d.Ns > 1) {
         const uint32_t kq = fdiv(j, d.div_Ns);
         const uint32_t k = j - kq * d.Ns;
@@ -625,6 +631,15 @@ __device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint3
                 if (g + u < P) v[g + u] = cmul(v[g + u], w[u]);
         }
     }
+}
+
+// Loads the P inputs of one butterfly of the first inner pass straight from
+// global memory: prologue, then the outer twiddle.
+template <int P>
+__device__ __forceinline__ void fused_load(const PassDesc& d, uint32_t bs, uint32_t j, uint32_t jj,
+                                           uint32_t m, vec2_t* v) {
+    prologue_load<P>(d, bs, j, jj, m, v);
+    outer_twiddle<P>(d, j, jj, m, v);
 }
 
 // Stores the P outputs of one butterfly of the last inner pass straight to
@@ -1013,6 +1028,102 @@ __device__ __forceinline__ void tile_body_spec(const PassDesc& d, uint32_t lane0
         spec_stage<16, R, 16, IO_SMEM, IO_SMEM, INV>(d, bufA, bufB, lane0, total);
         __syncthreads();
         spec_stage<PL, R, 256, IO_SMEM, IO_GLOBAL, INV>(d, bufB, nullptr, lane0, total);
+    }
+}
+
+// A CTA that runs many tiles of one power-of-two pass in turn, with the
+// global loads of its next tile's first stage issued before the current
+// tile's arithmetic, so the HBM latency of one tile hides behind the work of
+// the previous one.  Needs a plain prologue (no chirp or gather): the loads
+// are raw and the outer twiddle is applied when the tile's turn comes.
+// Every tile's first stage has at most one radix-16 butterfly per thread
+// (C * R <= 4096 points, 256 threads).
+template <uint32_t R, bool INV>
+__device__ __forceinline__ void tile_loop_pipelined(const PassDesc& d, vec2_t* sm) {
+    constexpr uint32_t L = ilog2(R);
+    constexpr uint32_t K16 = L / 4;
+    constexpr int T = 1 << (L % 4);
+    constexpr int NP = int(K16) + (T > 1 ? 1 : 0);
+    constexpr int PL = T > 1 ? T : 16;
+    constexpr uint32_t M0 = R / 16;
+    const uint32_t total = d.batch * d.lanes_j;
+    vec2_t* bufA = sm;
+    vec2_t* bufB = sm + pad(d.C * R) + 1;
+    const uint32_t it = threadIdx.x;
+    const bool act = it < d.C * M0;
+    uint32_t c0, jj0;
+    if (d.load_mode == MODE_LANE) {
+        jj0 = fdiv(it, d.div_C);
+        c0 = it - jj0 * d.C;
+    } else {
+        c0 = it / M0;
+        jj0 = it % M0;
+    }
+    auto locate = [&](uint32_t tile, uint32_t& bs, uint32_t& j) -> bool {
+        const uint32_t g = tile * d.C + c0;
+        if (!act || g >= total) return false;
+        if (d.order == ORDER_J) {
+            bs = fdiv(g, d.div_lanes_j);
+            j = g - bs * d.lanes_j;
+        } else {
+            j = fdiv(g, d.div_batch);
+            bs = g - j * d.batch;
+        }
+        return true;
+    };
+    vec2_t nxt[16];
+    uint32_t bs_n = 0, j_n = 0;
+    bool live_n = false;
+    uint32_t tile = blockIdx.x;
+    if (tile < d.tiles) {
+        live_n = locate(tile, bs_n, j_n);
+        if (live_n) prologue_load<16>(d, bs_n, j_n, jj0, M0, nxt);
+    }
+    for (; tile < d.tiles; tile += gridDim.x) {
+        vec2_t v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = nxt[q];
+        const uint32_t bs = bs_n, j = j_n;
+        const bool live = live_n;
+        const uint32_t nt = tile + gridDim.x;
+        if (nt < d.tiles) {
+            live_n = locate(nt, bs_n, j_n);
+            if (live_n) prologue_load<16>(d, bs_n, j_n, jj0, M0, nxt);
+        }
+        const uint32_t lane0 = tile * d.C;
+        // first stage (radix 16, NS = 1): outer twiddle, butterfly, store
+        if (act) {
+            if (live) {
+                outer_twiddle<16>(d, j, jj0, M0, v);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = {real_t(0), real_t(0)};
+            }
+            dft<16, INV>(v);
+            const uint32_t ob = jj0 * 16;
+            if constexpr (NP == 1) {
+                if (live) fused_store<16>(d, bs, j, ob, 1, v);
+            } else {
+                if constexpr (kPadShift >= 4) {
+                    vec2_t* p0 = bufA + pad(c0 * R + ob);  // 16 slots inside one pad period
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) p0[q] = v[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) bufA[pad(c0 * R + ob + q)] = v[q];
+                }
+            }
+        }
+        if constexpr (NP == 2) {
+            __syncthreads();
+            spec_stage<PL, R, 16, IO_SMEM, IO_GLOBAL, INV>(d, bufA, nullptr, lane0, total);
+        } else if constexpr (NP == 3) {
+            __syncthreads();
+            spec_stage<16, R, 16, IO_SMEM, IO_SMEM, INV>(d, bufA, bufB, lane0, total);
+            __syncthreads();
+            spec_stage<PL, R, 256, IO_SMEM, IO_GLOBAL, INV>(d, bufB, nullptr, lane0, total);
+        }
+        __syncthreads();  // the next tile's first stage overwrites bufA
     }
 }
 
