@@ -229,6 +229,8 @@ UNIFORM_WORKLOADS = {
     "c2c_f32_2p24": lambda lib: Uniform(lib, 1 << 24, 1, "float", 3, "normal"),
     "c2c_f64_2p18x64": lambda lib: Uniform(lib, 1 << 18, 64, "double", 3, "normal"),
     "c2c_f32_4096x4096": lambda lib: Uniform(lib, 4096, 4096, "float", 1, "uniform"),
+    "c2c_f32_2p20x16": lambda lib: Uniform(lib, 1 << 20, 16, "float", 3, "normal"),
+    "c2c_f64_4096x4096": lambda lib: Uniform(lib, 4096, 4096, "double", 1, "uniform"),
 }
 
 
@@ -565,7 +567,9 @@ def main():
     e2e_val = ws * wl.flops_per_step() / (e2e_ms / 1e3) / 1e9
 
     peak, peak_kind = measured_peaks()
-    roof = dominant_kernel_roofline(wl, ms, lib, peak, peak_kind)
+    roof = dominant_kernel_roofline(wl, ms, lib, peak, peak_kind,
+                                    launches_per_step=launches / max(args.steps, 1),
+                                    workload=args.workload)
     line = {"metric": "5N*log2N GFLOP/s", "value": round(value, 2), "unit": "GFLOP/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -604,25 +608,40 @@ def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, devi
     return ms, world * flops_per_step / (ms / 1e3) / 1e9
 
 
-def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind):
-    per = wl.algorithmic_bytes_per_launch()
-    n = wl.launches_per_step()
+# DRAM bytes per launch of the dominant kernel from ncu captures
+# (dram__bytes_read.sum + dram__bytes_write.sum).  The uneven batch is too
+# large for a full-set capture: every 8th sequence was captured (37.47 M
+# points, 2.099 GB) and scaled by points, which the same length mix allows.
+NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.099e9 / 37465227}
+NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 219.3e6, "c2c_f32_2p18x64": 226.7e6}
+
+
+def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_step=None,
+                             workload=""):
+    """Roofline of the dominant kernel: algorithmic bytes of one launch (read +
+    write every point it transforms once) over the average launch time."""
+    es = 8 if wl.precision == "float" else 16
     if hasattr(wl, "algorithmic_bytes_per_step"):
-        achieved = wl.algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9
+        # uniform batches: every pass launch reads and writes every point once
+        n = max(1, int(round(launches_per_step or 1)))
+        per_launch = 2 * wl.N * wl.B * es
+        dur = ms_step / n
+        achieved = per_launch / (dur / 1e3) / 1e9
+        per_transform = wl.algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9
+        traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(workload)
         return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                "kernel": "k_pass_reg / k_pass (all passes of the step)"}
-    if per is None or not n:
-        total_bytes = wl.total * (8 if wl.precision == "float" else 16) * 2
-        achieved = total_bytes / (ms_step / 1e3) / 1e9
-        return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
-                "peak_source": peak_kind, "kernel": "k_persistent (all passes of the batch)"}
-    dur = ms_step / n
-    achieved = per / (dur / 1e3) / 1e9
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "k_pass_reg / k_pass_pipe (one launch per pass)",
+                "launches_per_step": n, "launch_ms": round(dur, 4),
+                "per_transform_gbs": round(per_transform, 1)}
+    # the uneven batch: one k_persistent launch runs every pass of every sequence
+    total_bytes = wl.total * es * 2
+    achieved = total_bytes / (ms_step / 1e3) / 1e9
+    ratio = NCU_DRAM_BYTES_PER_POINT.get(f"uneven_{wl.precision}")
+    traffic = round(ratio * wl.total) if ratio else None
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-            "kernel": "k_pass", "launch_ms": round(dur, 4)}
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "peak_source": peak_kind, "kernel": "k_persistent (all passes of the batch)"}
 
 
 if __name__ == "__main__":

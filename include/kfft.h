@@ -368,6 +368,56 @@ typedef void* (*kfft_callback_malloc)(uint32_t sz);
 typedef void (*kfft_callback_free_null)(void** mem);
 typedef kfft_return_t (*kfft_callback_cleanup)(void* mem);
 typedef const char* (*kfft_callback_strerr)(const kfft_return_t code);
+/* incs/kfft_shift.h:29-36 */
+typedef void (*kfft_callback_shift_cpx)(kfft_cpx* buf, const uint32_t size, const bool is_inverse,
+                                        kfft_pool_t* mmgr);
+typedef void (*kfft_callback_shift_scalar)(kfft_scalar* buf, const uint32_t size,
+                                           const bool is_inverse, kfft_pool_t* mmgr);
+/* ext/2d/kfft_cpx2.h, ext/2d/kfft_scalar2.h (DYNAPI blocks) */
+typedef kfft_plan_c2d* (*kfft_callback_config2_cpx)(const uint32_t x_size, const uint32_t y_size,
+                                                    const uint32_t flags, kfft_pool_t* A,
+                                                    size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval2_cpx)(kfft_plan_c2d* cfg, const kfft_cpx* fin,
+                                                 kfft_cpx* fout);
+typedef void (*kfft_callback_shift2_cpx)(kfft_cpx* buf, kfft_cpx* ftmp, const uint32_t sz_x,
+                                         const uint32_t sz_y, const bool is_inverse,
+                                         kfft_pool_t* mmgr);
+typedef kfft_plan_s2d* (*kfft_callback_config2_scalar)(const uint32_t x_size,
+                                                       const uint32_t y_size, const uint32_t flags,
+                                                       kfft_pool_t* A, size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval2_scalar)(kfft_plan_s2d* plan, const kfft_scalar* fin,
+                                                    kfft_cpx* fout);
+typedef kfft_return_t (*kfft_callback_evali2_scalar)(kfft_plan_s2d* plan, const kfft_cpx* fin,
+                                                     kfft_scalar* fout);
+typedef void (*kfft_callback_shift2_scalar)(kfft_scalar* buf, kfft_scalar* ftmp,
+                                            const uint32_t sz_x, const uint32_t sz_y,
+                                            const bool is_inverse, kfft_pool_t* mmgr);
+/* ext/conv/kfft_cpx_conv.h, ext/conv/kfft_scalar_conv.h (DYNAPI blocks) */
+typedef kfft_plan_ccnv* (*kfft_callback_config_conv_cpx)(const uint32_t nfft, const uint32_t flags,
+                                                         kfft_pool_t* A, size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval_conv_cpx)(kfft_plan_ccnv* plan, const kfft_cpx* fin_A,
+                                                     const kfft_cpx* fin_B, kfft_cpx* fout);
+typedef kfft_plan_scnv* (*kfft_callback_config_conv_scalar)(const uint32_t nfft,
+                                                            const uint32_t flags, kfft_pool_t* A,
+                                                            size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval_conv_scalar)(kfft_plan_scnv* plan,
+                                                        const kfft_scalar* fin_A,
+                                                        const kfft_scalar* fin_B,
+                                                        kfft_scalar* fout);
+/* ext/conv2d/kfft_cpx_conv.h, ext/conv2d/kfft_scalar_conv.h (DYNAPI blocks) */
+typedef kfft_plan_c2cnv* (*kfft_callback_config_conv2_cpx)(const uint32_t x, const uint32_t y,
+                                                           const uint32_t flags, kfft_pool_t* A,
+                                                           size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval_conv2_cpx)(kfft_plan_c2cnv* plan,
+                                                      const kfft_cpx* fin_A,
+                                                      const kfft_cpx* fin_B, kfft_cpx* fout);
+typedef kfft_plan_s2cnv* (*kfft_callback_config_conv2_scalar)(const uint32_t x, const uint32_t y,
+                                                              const uint32_t flags,
+                                                              kfft_pool_t* A, size_t* lenmem);
+typedef kfft_return_t (*kfft_callback_eval_conv2_scalar)(kfft_plan_s2cnv* plan,
+                                                         const kfft_scalar* fin_A,
+                                                         const kfft_scalar* fin_B,
+                                                         kfft_scalar* fout);
 
 #ifdef __cplusplus
 }

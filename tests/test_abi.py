@@ -114,3 +114,39 @@ def test_no_cpu_fallback_without_gpu(clib):
     assert not clib.L.kfft_config_cpx(64, 0, None, None)
     assert "no CUDA device" in clib.last_error()
     assert clib.stats().device == -1
+
+
+DYNAPI_NAMES = ["config_cpx", "eval_cpx", "config_scalar", "eval_scalar", "evali_scalar", "info",
+                "next_fast_size", "malloc", "free_null", "cleanup", "strerr", "shift_cpx",
+                "shift_scalar", "config2_cpx", "eval2_cpx", "shift2_cpx", "config2_scalar",
+                "eval2_scalar", "evali2_scalar", "shift2_scalar", "config_conv_cpx",
+                "eval_conv_cpx", "config_conv_scalar", "eval_conv_scalar", "config_conv2_cpx",
+                "eval_conv2_cpx", "config_conv2_scalar", "eval_conv2_scalar"]
+# callback name -> exported function, where the two differ
+DYNAPI_TARGET = {"config_conv2_cpx": "config2_conv_cpx", "eval_conv2_cpx": "eval2_conv_cpx",
+                 "config_conv2_scalar": "config2_conv_scalar",
+                 "eval_conv2_scalar": "eval2_conv_scalar"}
+
+
+@pytest.mark.parametrize("half", [False, True])
+def test_dynapi_callback_types_match_the_functions(tmp_path, half):
+    """Every DYNAPI callback typedef (the reference's function-pointer types for
+    dynamic loading) is assignable from the engine's function without a cast,
+    in both precision builds, and the program links."""
+    import shutil
+    import subprocess
+    lines = ['#include "kfft.h"', "int main(void) {"]
+    for n in DYNAPI_NAMES:
+        f = "kfft_" + DYNAPI_TARGET.get(n, n)
+        lines.append(f"    kfft_callback_{n} p_{n} = {f}; (void)p_{n};")
+    lines += ["    return 0;", "}"]
+    (tmp_path / "d.c").write_text("\n".join(lines) + "\n")
+    lib = kfft_gb300.library_path("float" if half else "double")
+    if not os.path.isfile(lib) or shutil.which("gcc") is None:
+        pytest.skip("engine library or gcc missing")
+    cmd = ["gcc", "-std=c11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+           str(tmp_path / "d.c"), "-o", str(tmp_path / "d"), lib]
+    if half:
+        cmd.insert(1, "-DKFFT_HALF_SCALAR")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
