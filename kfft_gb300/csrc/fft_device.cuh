@@ -1173,6 +1173,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     }
     vec2_t* bufA = sm;
     vec2_t* bufB = sm + pad(d.C * d.R) + 1;
+#if defined(KFFT_HALF_SCALAR)
     switch (d.spec) {
         case 4: tile_body_spec<16, INV>(d, lane0, total, bufA, bufB); return;
         case 5: tile_body_spec<32, INV>(d, lane0, total, bufA, bufB); return;
@@ -1185,6 +1186,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
         case 12: tile_body_spec<4096, INV>(d, lane0, total, bufA, bufB); return;
         default: break;
     }
+#endif
     const vec2_t* src = nullptr;
 #if defined(KFFT_HALF_SCALAR)
     TcFrag Fr, Fi, Gm;

@@ -585,12 +585,16 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     while (!d.regmode && C > 1 && smem_for(C * s.R) > kSmemBudget) --C;
     d.C = C;
     // power-of-two register tiles of 16..4096 points run a compile-time body
+    // (FP32 only: in FP64 its fully unrolled stages spill and the FP64 pipe,
+    // not index arithmetic, bounds the pass)
     d.spec = 0;
+#if defined(KFFT_HALF_SCALAR)
     if (d.regmode && !d.tc && s.R >= 16 && s.R <= 4096 && (s.R & (s.R - 1)) == 0) {
         uint32_t l = 0;
         while ((1u << l) < s.R) ++l;
         d.spec = uint8_t(l);
     }
+#endif
     const uint64_t lanes = uint64_t(d.batch) * d.lanes_j;
     d.tiles = uint32_t((lanes + C - 1) / C);
     uint32_t elems = C * s.R;
