@@ -261,6 +261,54 @@ struct EvalGuard {
     explicit EvalGuard(kfft_gpu_plan* g) : lk(*g->mu) {}
 };
 
+// Copy streams of this host thread for the chunked host-buffer path: copies
+// in, compute and copies out of successive chunks overlap.
+struct CopyStreams {
+    cudaStream_t in = nullptr, out = nullptr;
+};
+
+CopyStreams* copy_streams() {
+    thread_local CopyStreams cs;
+    if (!cs.in) {
+        if (cudaStreamCreateWithFlags(&cs.in, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&cs.out, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            cs.in = cs.out = nullptr;
+            return nullptr;
+        }
+    }
+    return &cs;
+}
+
+// Number of chunks a host-buffer batch of `bytes` in `batch` sequences is
+// split into so that its copies overlap the transform (1: no split).
+uint32_t host_chunks(size_t bytes, uint32_t batch) {
+    constexpr size_t kChunkBytes = size_t(32) << 20;
+    if (batch < 2 || bytes < 2 * kChunkBytes) return 1;
+    size_t k = bytes / kChunkBytes;
+    if (k > 8) k = 8;
+    if (k > batch) k = batch;
+    return uint32_t(k);
+}
+
+// Events of one chunked call (released when the call returns; the stream
+// waits recorded on them have been enqueued by then).
+struct EventSet {
+    std::vector<cudaEvent_t> ev;
+    cudaEvent_t get() {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        ev.push_back(e);
+        return e;
+    }
+    ~EventSet() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+};
+
 }  // namespace
 
 // ===========================================================================
@@ -503,13 +551,50 @@ KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* 
     vec2_t* stage_in = nullptr;
     if (hin) {
         stage_in = static_cast<vec2_t*>(cv.take(bytes));
-        cudaMemcpyAsync(stage_in, fin, bytes, cudaMemcpyHostToDevice, st);
         din = stage_in;
     }
     if (hout) dout = (hin && fin == fout) ? stage_in : static_cast<vec2_t*>(cv.take(bytes));
     void* w = cv.take(wsb);
-    if (!run_cpx(P, din, dout, batch, inverse_scale(plan->flags, plan->nfft), w, wsb, st))
-        return KFFT_RET_BUFFER_FAIL;
+    const real_t scale = inverse_scale(plan->flags, plan->nfft);
+    const uint32_t chunks = (hin || hout) ? host_chunks(bytes, batch) : 1;
+    CopyStreams* cs = chunks > 1 ? copy_streams() : nullptr;
+    if (cs) {
+        // chunk k's copy in, transform and copy out overlap the neighbouring
+        // chunks' (sequences are independent; the workspace serves one chunk
+        // at a time on the compute stream)
+        EventSet evs;
+        const size_t per = sizeof(vec2_t) * size_t(P.N);
+        for (uint32_t k = 0; k < chunks; ++k) {
+            const uint32_t b0 = uint32_t(uint64_t(batch) * k / chunks);
+            const uint32_t b1 = uint32_t(uint64_t(batch) * (k + 1) / chunks);
+            const size_t off = size_t(b0) * P.N, cb = per * (b1 - b0);
+            if (hin) {
+                cudaMemcpyAsync(stage_in + off, fin + off, cb, cudaMemcpyHostToDevice, cs->in);
+                cudaEvent_t e = evs.get();
+                if (!e) return KFFT_RET_BUFFER_FAIL;
+                cudaEventRecord(e, cs->in);
+                cudaStreamWaitEvent(st, e, 0);
+            }
+            if (!run_cpx(P, din + off, dout + off, b1 - b0, scale, w, wsb, st))
+                return KFFT_RET_BUFFER_FAIL;
+            if (hout) {
+                cudaEvent_t e = evs.get();
+                if (!e) return KFFT_RET_BUFFER_FAIL;
+                cudaEventRecord(e, st);
+                cudaStreamWaitEvent(cs->out, e, 0);
+                cudaMemcpyAsync(fout + off, dout + off, cb, cudaMemcpyDeviceToHost, cs->out);
+            }
+        }
+        if (hout) {
+            cudaEvent_t e = evs.get();
+            if (!e) return KFFT_RET_BUFFER_FAIL;
+            cudaEventRecord(e, cs->out);
+            cudaStreamWaitEvent(st, e, 0);
+        }
+        return finish(st);
+    }
+    if (hin) cudaMemcpyAsync(stage_in, fin, bytes, cudaMemcpyHostToDevice, st);
+    if (!run_cpx(P, din, dout, batch, scale, w, wsb, st)) return KFFT_RET_BUFFER_FAIL;
     if (hout) cudaMemcpyAsync(fout, dout, bytes, cudaMemcpyDeviceToHost, st);
     return finish(st);
 }

@@ -33,17 +33,12 @@ struct Item {
 };
 }  // namespace
 
-struct kfft_plan_uneven {
-    uint32_t flags = 0;
-    std::vector<uint32_t> lengths;
-    std::vector<uint64_t> offsets;
-    uint64_t total = 0;
-    DeviceArena arena;
-    std::map<uint32_t, std::unique_ptr<FftPlan>> plans;
-    void* ws = nullptr;
-    size_t ws_bytes = 0;
-    void* stage = nullptr;  // host staging: in and out, total points each
-    // queue recorded for (in, out)
+// One recorded work queue over a range of sequences: descriptors, items and
+// counters in device memory, and the graph (counter reset + persistent
+// kernel) that replays it for one (in, out) pair.
+struct UnevenQueue {
+    size_t s0 = 0, s1 = 0;  // sequences [s0, s1)
+    uint64_t p0 = 0, p1 = 0;  // their points [p0, p1)
     const void* g_in = nullptr;
     void* g_out = nullptr;
     void* qmem = nullptr;  // descs | extras | deps | items | counters
@@ -52,8 +47,7 @@ struct kfft_plan_uneven {
     size_t counter_bytes = 0;
     cudaGraphExec_t exec = nullptr;
     uint32_t ndesc = 0, nitems = 0;
-    std::mutex mu;
-    void drop_queue() {
+    void drop() {
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
         if (qmem) {
@@ -62,9 +56,28 @@ struct kfft_plan_uneven {
         }
         qmem = nullptr;
         qbytes = 0;
+        g_in = nullptr;
+        g_out = nullptr;
     }
+};
+
+struct kfft_plan_uneven {
+    uint32_t flags = 0;
+    std::vector<uint32_t> lengths;
+    std::vector<uint64_t> offsets;
+    std::vector<size_t> ws_offsets;  // workspace slice of each sequence
+    uint64_t total = 0;
+    DeviceArena arena;
+    std::map<uint32_t, std::unique_ptr<FftPlan>> plans;
+    void* ws = nullptr;
+    size_t ws_bytes = 0;
+    void* stage = nullptr;  // host staging: in and out, total points each
+    UnevenQueue whole;                // the whole batch, for device buffers
+    std::vector<UnevenQueue> groups;  // contiguous groups, for host buffers
+    std::mutex mu;
     ~kfft_plan_uneven() {
-        drop_queue();
+        whole.drop();
+        for (UnevenQueue& q : groups) q.drop();
         if (ws) {
             cudaFree(ws);
             account_device_bytes(-int64_t(ws_bytes));
@@ -84,23 +97,20 @@ real_t scale_for(uint32_t flags, uint32_t n) {
 
 size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Builds every sequence's pass chain, the dependency table and the level-ordered
-// queue, uploads them and records the graph.
-bool record(kfft_plan_uneven* P, const vec2_t* in, vec2_t* out) {
+// Builds the pass chain of every sequence of Q's range, the dependency table
+// and the level-ordered queue, uploads them and records the graph.
+bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) {
     std::vector<PassDesc> all;
     std::vector<int32_t> deps;
     std::vector<uint32_t> level;
     char* base = static_cast<char*>(P->ws);
-    size_t used = 0;
-    for (size_t i = 0; i < P->lengths.size(); ++i) {
+    for (size_t i = Q.s0; i < Q.s1; ++i) {
         const uint32_t n = P->lengths[i];
         if (n == 0) continue;
         const FftPlan& fp = *P->plans[n];
-        size_t wb = workspace_bytes(fp, 1);
         Workspace ws;
-        ws.base = base + used;
-        ws.size = wb;
-        used += a256(wb);
+        ws.base = base + P->ws_offsets[i];
+        ws.size = workspace_bytes(fp, 1);
         Layout l;
         l.batch = 1;
         l.bs = n;
@@ -134,21 +144,21 @@ bool record(kfft_plan_uneven* P, const vec2_t* in, vec2_t* out) {
     const size_t b_dep = a256(sizeof(int32_t) * nd);
     const size_t b_item = a256(sizeof(Item) * items.size());
     const size_t b_cnt = a256(sizeof(uint32_t) * (nd + 2));
-    P->drop_queue();
-    P->qbytes = b_desc + b_extra + b_dep + b_item + b_cnt;
-    if (cudaMalloc(&P->qmem, P->qbytes) != cudaSuccess) {
+    Q.drop();
+    Q.qbytes = b_desc + b_extra + b_dep + b_item + b_cnt;
+    if (cudaMalloc(&Q.qmem, Q.qbytes) != cudaSuccess) {
         cudaGetLastError();
-        P->qmem = nullptr;
+        Q.qmem = nullptr;
         return false;
     }
-    account_device_bytes(int64_t(P->qbytes));
-    char* q = static_cast<char*>(P->qmem);
+    account_device_bytes(int64_t(Q.qbytes));
+    char* q = static_cast<char*>(Q.qmem);
     PassDesc* d_desc = reinterpret_cast<PassDesc*>(q);
     void* d_extra = q + b_desc;
     int32_t* d_dep = reinterpret_cast<int32_t*>(q + b_desc + b_extra);
     Item* d_item = reinterpret_cast<Item*>(q + b_desc + b_extra + b_dep);
-    P->counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_dep + b_item);
-    P->counter_bytes = sizeof(uint32_t) * (nd + 2);
+    Q.counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_dep + b_item);
+    Q.counter_bytes = sizeof(uint32_t) * (nd + 2);
     std::vector<char> extras(pass_extra_bytes() * nd);
     fill_extras(all.data(), extras.data(), nd);
     cudaStream_t st = cudaStreamPerThread;
@@ -157,30 +167,31 @@ bool record(kfft_plan_uneven* P, const vec2_t* in, vec2_t* out) {
     cudaMemcpyAsync(d_dep, deps.data(), sizeof(int32_t) * nd, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_item, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return false;
-    P->ndesc = nd;
-    P->nitems = uint32_t(items.size());
+    Q.ndesc = nd;
+    Q.nitems = uint32_t(items.size());
 
     cudaStream_t cap;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return false;
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaMemsetAsync(P->counters, 0, P->counter_bytes, cap);
-        launch_persistent(d_desc, d_extra, d_dep, d_item, P->nitems, P->counters,
-                          P->counters + 2, P->counters + 1, smem, cap);
+        cudaMemsetAsync(Q.counters, 0, Q.counter_bytes, cap);
+        if (Q.nitems)
+            launch_persistent(d_desc, d_extra, d_dep, d_item, Q.nitems, Q.counters,
+                              Q.counters + 2, Q.counters + 1, smem, cap);
         e = cudaStreamEndCapture(cap, &graph);
     }
-    count_launch(-1);  // counted on every replay instead
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&P->exec, graph, 0);
+    if (Q.nitems) count_launch(-1);  // counted on every replay instead
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&Q.exec, graph, 0);
     if (graph) cudaGraphDestroy(graph);
     cudaStreamDestroy(cap);
     if (e != cudaSuccess) {
         note_cuda_error(e);
-        P->exec = nullptr;
+        Q.exec = nullptr;
         return false;
     }
-    P->g_in = in;
-    P->g_out = out;
+    Q.g_in = in;
+    Q.g_out = out;
     return true;
 }
 
@@ -193,19 +204,66 @@ bool is_dev(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-kfft_return_t launch(kfft_plan_uneven* P, const vec2_t* in, vec2_t* out, cudaStream_t st) {
-    if (!P->exec || P->g_in != in || P->g_out != out) {
-        if (!record(P, in, out)) return KFFT_RET_BUFFER_FAIL;
+// copy streams of this host thread for the host-buffer path
+struct CopyPair {
+    cudaStream_t in = nullptr, out = nullptr;
+};
+
+CopyPair* copy_pair() {
+    thread_local CopyPair cp;
+    if (!cp.in) {
+        if (cudaStreamCreateWithFlags(&cp.in, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&cp.out, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            cp.in = cp.out = nullptr;
+            return nullptr;
+        }
     }
-    cudaError_t e = cudaGraphLaunch(P->exec, st);
+    return &cp;
+}
+
+kfft_return_t launch(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out,
+                     cudaStream_t st) {
+    if (!Q.exec || Q.g_in != in || Q.g_out != out) {
+        if (!record(P, Q, in, out)) return KFFT_RET_BUFFER_FAIL;
+    }
+    cudaError_t e = cudaGraphLaunch(Q.exec, st);
     count_graph_launch();
-    count_launch(1);
+    if (Q.nitems) count_launch(1);
     if (e != cudaSuccess) {
         note_cuda_error(e);
         return KFFT_RET_BUFFER_FAIL;
     }
     return KFFT_RET_SUCCESS;
 }
+
+// Contiguous groups of about equal points for the host-buffer path: copies
+// of one group overlap the transform of its neighbours.
+void make_groups(kfft_plan_uneven* P) {
+    constexpr uint64_t kGroupPoints = uint64_t(1) << 24;
+    const size_t count = P->lengths.size();
+    const uint64_t k = std::min<uint64_t>(8, P->total / kGroupPoints);
+    if (k < 2 || count < 2) return;
+    std::vector<std::pair<size_t, size_t>> ranges;
+    size_t s = 0;
+    for (uint64_t g = 0; g < k && s < count; ++g) {
+        const size_t s0 = s;
+        const uint64_t target = P->total * (g + 1) / k;
+        if (g + 1 == k) s = count;
+        while (s < count && (s == s0 || P->offsets[s] + P->lengths[s] <= target)) ++s;
+        ranges.push_back({s0, s});
+    }
+    if (ranges.size() < 2 || ranges.back().second != count) return;
+    P->groups.resize(ranges.size());
+    for (size_t g = 0; g < ranges.size(); ++g) {
+        UnevenQueue& Q = P->groups[g];
+        Q.s0 = ranges[g].first;
+        Q.s1 = ranges[g].second;
+        Q.p0 = P->offsets[Q.s0];
+        Q.p1 = Q.s1 < count ? P->offsets[Q.s1] : P->total;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -218,6 +276,7 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
     P->flags = flags;
     P->lengths.assign(lengths, lengths + count);
     P->offsets.resize(count);
+    P->ws_offsets.assign(count, 0);
     const int sign = (flags & KFFT_FLAG_INVERSE) ? +1 : -1;
     cudaStream_t st = cudaStreamPerThread;
     size_t ws = 0;
@@ -231,8 +290,13 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
             if (!fp) return NULL;
             P->plans[n].reset(fp);
         }
+        P->ws_offsets[i] = ws;
         ws += a256(workspace_bytes(*P->plans[n], 1));
     }
+    P->whole.s0 = 0;
+    P->whole.s1 = count;
+    P->whole.p1 = P->total;
+    make_groups(P.get());
     if (ws) {
         if (cudaMalloc(&P->ws, ws) != cudaSuccess) {
             cudaGetLastError();
@@ -253,7 +317,7 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven_async(kfft_plan_uneven* plan, const 
     if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
     std::lock_guard<std::mutex> lk(plan->mu);
     cudaSetDevice(current_device());
-    kfft_return_t r = launch(plan, reinterpret_cast<const vec2_t*>(fin),
+    kfft_return_t r = launch(plan, plan->whole, reinterpret_cast<const vec2_t*>(fin),
                              reinterpret_cast<vec2_t*>(fout), static_cast<cudaStream_t>(stream));
     if (take_pending_error()) return KFFT_RET_BUFFER_FAIL;
     return r;
@@ -278,18 +342,76 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_c
     }
     vec2_t* s_in = static_cast<vec2_t*>(plan->stage);
     vec2_t* s_out = s_in ? s_in + plan->total : nullptr;
-    if (hin) {
-        cudaMemcpyAsync(s_in, fin, bytes, cudaMemcpyHostToDevice, st);
-        din = s_in;
-    }
+    if (hin) din = s_in;
     if (hout) dout = s_out;
-    kfft_return_t r = launch(plan, din, dout, st);
-    if (r != KFFT_RET_SUCCESS) return r;
-    if (hout) cudaMemcpyAsync(fout, dout, bytes, cudaMemcpyDeviceToHost, st);
+    std::vector<UnevenQueue*> used;
+    CopyPair* cp = ((hin || hout) && !plan->groups.empty()) ? copy_pair() : nullptr;
+    if (cp) {
+        // group g's copy in, transform and copy out overlap its neighbours'
+        std::vector<cudaEvent_t> evs;
+        auto event = [&]() {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                return (cudaEvent_t) nullptr;
+            }
+            evs.push_back(e);
+            return e;
+        };
+        kfft_return_t r = KFFT_RET_SUCCESS;
+        for (UnevenQueue& Q : plan->groups) {
+            const size_t gb = sizeof(vec2_t) * (Q.p1 - Q.p0);
+            if (hin) {
+                cudaMemcpyAsync(s_in + Q.p0, fin + Q.p0, gb, cudaMemcpyHostToDevice, cp->in);
+                cudaEvent_t e = event();
+                if (!e) {
+                    r = KFFT_RET_BUFFER_FAIL;
+                    break;
+                }
+                cudaEventRecord(e, cp->in);
+                cudaStreamWaitEvent(st, e, 0);
+            }
+            r = launch(plan, Q, din, dout, st);
+            if (r != KFFT_RET_SUCCESS) break;
+            used.push_back(&Q);
+            if (hout) {
+                cudaEvent_t e = event();
+                if (!e) {
+                    r = KFFT_RET_BUFFER_FAIL;
+                    break;
+                }
+                cudaEventRecord(e, st);
+                cudaStreamWaitEvent(cp->out, e, 0);
+                cudaMemcpyAsync(fout + Q.p0, s_out + Q.p0, gb, cudaMemcpyDeviceToHost, cp->out);
+            }
+        }
+        if (hout) {
+            cudaEvent_t e = event();
+            if (e) {
+                cudaEventRecord(e, cp->out);
+                cudaStreamWaitEvent(st, e, 0);
+            }
+        }
+        cudaError_t se = cudaStreamSynchronize(st);
+        for (cudaEvent_t e : evs) cudaEventDestroy(e);
+        if (se != cudaSuccess) note_cuda_error(se);
+        if (r != KFFT_RET_SUCCESS) return r;
+    } else {
+        if (hin) cudaMemcpyAsync(s_in, fin, bytes, cudaMemcpyHostToDevice, st);
+        kfft_return_t r = launch(plan, plan->whole, din, dout, st);
+        if (r != KFFT_RET_SUCCESS) return r;
+        used.push_back(&plan->whole);
+        if (hout) cudaMemcpyAsync(fout, dout, bytes, cudaMemcpyDeviceToHost, st);
+    }
+    // the queue kernel's error word: set when a dependency wait gave up
     uint32_t err = 0;
-    cudaMemcpyAsync(&err, plan->counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) note_cuda_error(e);
+    for (UnevenQueue* Q : used) {
+        uint32_t e1 = 0;
+        cudaMemcpyAsync(&e1, Q->counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) note_cuda_error(e);
+        err |= e1;
+    }
     if (take_pending_error() || err) return KFFT_RET_BUFFER_FAIL;
     return KFFT_RET_SUCCESS;
 }
