@@ -142,6 +142,15 @@ KFFT_API kfft_return_t kfft_mlp_train(kfft_mlp* m, const float* X, const float* 
                                       uint32_t epochs, uint32_t minibatch, float lr,
                                       uint64_t seed, float* loss);
 
+/*
+ * Failure-detection check of the uneven-batch queue kernel, without a GPU
+ * fault: runs a queue of empty passes whose dependency is (satisfiable != 0)
+ * or is not (0) ever met, with dependency waits limited to max_polls polls of
+ * about 200 ns.  Returns the kernel's error word (0: every wait succeeded,
+ * 1: a wait gave up and the kernel returned) or -1 on a CUDA error.
+ */
+KFFT_API int kfft_gb300_queue_selftest(uint32_t max_polls, int satisfiable);
+
 /* Engine introspection (used by tests and the benchmark). */
 typedef struct {
     uint64_t kernel_launches; /* kernels this library launched since load */

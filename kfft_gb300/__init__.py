@@ -60,7 +60,7 @@ EXPORTED_SYMBOLS = [
     "kfft_variant_count", "kfft_config_cpx_variant", "kfft_tune_set", "kfft_tune_get",
     "kfft_tune_clear",
     "kfft_mlp_create", "kfft_mlp_release", "kfft_mlp_params", "kfft_mlp_get", "kfft_mlp_set",
-    "kfft_mlp_predict", "kfft_mlp_loss_grad", "kfft_mlp_train",
+    "kfft_mlp_predict", "kfft_mlp_loss_grad", "kfft_mlp_train", "kfft_gb300_queue_selftest",
 ]
 
 
@@ -196,6 +196,8 @@ class KfftLib:
         L.kfft_mlp_train.restype = ctypes.c_uint
         L.kfft_mlp_train.argtypes = [vp, vp, vp, u32, u32, u32, ctypes.c_float, ctypes.c_uint64,
                                      fp]
+        L.kfft_gb300_queue_selftest.restype = ctypes.c_int
+        L.kfft_gb300_queue_selftest.argtypes = [u32, ctypes.c_int]
         L.kfft_gb300_last_error.restype = ctypes.c_char_p
         L.kfft_gb300_describe.restype = ctypes.c_char_p
         L.kfft_gb300_describe.argtypes = [vp]

@@ -135,9 +135,13 @@ void launch_pass(const PassDesc& d, cudaStream_t st);
 // register-resident tile (PassDesc::regmode).
 size_t pass_extra_bytes();
 void fill_extras(const PassDesc* d, void* extras, size_t n);
+// A dependency wait polls at most max_polls times (about 200 ns apart) before
+// it sets the error word and skips the tile; the default allows about 3 s.
+constexpr uint32_t kQueueMaxPolls = 1u << 24;
 bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
                        const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
-                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st);
+                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st,
+                       uint32_t max_polls = kQueueMaxPolls);
 // Even-N real transform post-processing (kfft_scalar.c:174-216): z holds the
 // N/2-point spectrum of each sequence, out gets nbins bins per sequence.
 void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32_t h,

@@ -1225,8 +1225,8 @@ __device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {
 
 // Waits for all tiles of pass `dep` to finish; a bounded spin that reports
 // failure instead of hanging.
-__device__ __forceinline__ bool wait_for(const uint32_t* done, uint32_t need) {
-    for (uint32_t it = 0; it < (1u << 24); ++it) {
+__device__ __forceinline__ bool wait_for(const uint32_t* done, uint32_t need, uint32_t max_polls) {
+    for (uint32_t it = 0; it < max_polls; ++it) {
         if (load_acquire(done) >= need) return true;
         __nanosleep(200);
     }

@@ -8,7 +8,7 @@ namespace kfft {
 __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent(
     const PassDesc* __restrict__ descs, const PassExtra* __restrict__ extras,
     const int32_t* __restrict__ deps, const QueueItem* __restrict__ items, uint32_t nitems,
-    uint32_t* head, uint32_t* done, uint32_t* error) {
+    uint32_t* head, uint32_t* done, uint32_t* error, uint32_t max_polls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_item;
     __shared__ uint32_t s_ok;
@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
         if (threadIdx.x == 0) {
             bool ok = true;
             const int32_t dep = deps[q.desc];
-            if (dep >= 0) ok = wait_for(&done[dep], descs[dep].tiles);
+            if (dep >= 0) ok = wait_for(&done[dep], descs[dep].tiles, max_polls);
             if (!ok) atomicExch(error, 1u);
             s_ok = ok ? 1u : 0u;
         }
@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
 
 bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
                        const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
-                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st) {
+                       uint32_t* error, uint32_t smem_bytes, cudaStream_t st,
+                       uint32_t max_polls) {
     static int blocks_per_sm = -1;
     static uint32_t configured_smem = 0;
     static int sms = 0;
@@ -75,7 +76,7 @@ bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t*
     if (grid > nitems) grid = nitems ? nitems : 1;
     k_persistent<<<grid, kPassThreads, smem_bytes, st>>>(
         descs, static_cast<const PassExtra*>(extras), deps, static_cast<const QueueItem*>(items),
-        nitems, head, done, error);
+        nitems, head, done, error, max_polls);
     note_cuda_error(cudaGetLastError());
     count_launch();
     return true;

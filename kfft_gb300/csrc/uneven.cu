@@ -418,4 +418,58 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_c
 
 KFFT_API void kfft_release_uneven(kfft_plan_uneven* plan) { delete plan; }
 
+// Failure-detection check of the queue kernel without a GPU fault: a queue of
+// empty passes whose second item depends on the first.  With `satisfiable`
+// 0 the first item is left out of the queue, so the dependency counter is a
+// flag nothing sets: the wait gives up after max_polls polls, sets the error
+// word and the kernel returns.  Returns the error word, or -1 on a CUDA error.
+KFFT_API int kfft_gb300_queue_selftest(uint32_t max_polls, int satisfiable) {
+    if (!ensure_device()) return -1;
+    const size_t b_desc = a256(2 * sizeof(PassDesc));
+    const size_t b_extra = a256(2 * pass_extra_bytes());
+    const size_t b_dep = a256(2 * sizeof(int32_t));
+    const size_t b_item = a256(2 * sizeof(Item));
+    const size_t b_cnt = a256(4 * sizeof(uint32_t));
+    void* mem = nullptr;
+    if (cudaMalloc(&mem, b_desc + b_extra + b_dep + b_item + b_cnt) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    char* q = static_cast<char*>(mem);
+    PassDesc d[2];
+    memset(d, 0, sizeof(d));
+    for (PassDesc& x : d) {  // a length-1 pass over zero sequences: no memory access
+        x.tiles = 1;
+        x.C = 1;
+        x.lanes_j = 1;
+        x.batch = 0;
+        x.threads = kPassThreads;
+    }
+    const int32_t deps[2] = {-1, 0};
+    const Item items[2] = {{0, 0}, {1, 0}};
+    const Item* first = satisfiable ? items : items + 1;
+    const uint32_t nitems = satisfiable ? 2u : 1u;
+    std::vector<char> extras(2 * pass_extra_bytes(), 0);
+    cudaStream_t st = cudaStreamPerThread;
+    uint32_t* counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_dep + b_item);
+    cudaMemcpyAsync(q, d, sizeof(d), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(q + b_desc, extras.data(), extras.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(q + b_desc + b_extra, deps, sizeof(deps), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(q + b_desc + b_extra + b_dep, first, nitems * sizeof(Item),
+                    cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(counters, 0, 4 * sizeof(uint32_t), st);
+    launch_persistent(reinterpret_cast<PassDesc*>(q), q + b_desc,
+                      reinterpret_cast<int32_t*>(q + b_desc + b_extra), q + b_desc + b_extra + b_dep,
+                      nitems, counters, counters + 2, counters + 1, 0, st, max_polls);
+    uint32_t err = 0;
+    cudaMemcpyAsync(&err, counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(mem);
+    if (e != cudaSuccess || take_pending_error()) {
+        note_cuda_error(e);
+        return -1;
+    }
+    return int(err);
+}
+
 }  // extern "C"

@@ -74,3 +74,16 @@ def test_grouped_host_uneven_matches_device_path(libf):
             assert rel_l2(y[a:b], O.fft_cpx(x[a:b])) <= TOL32, int(lengths[i])
     finally:
         libf.L.kfft_release_uneven(p)
+
+
+def test_queue_wait_gives_up_and_reports(libf, lib):
+    """A dependency that is never met (a counter nothing increments) makes the
+    queue kernel's bounded wait give up, set its error word and return; the
+    context stays usable.  The control queue, whose dependency is met,
+    reports no error."""
+    for L in (libf, lib):
+        assert L.L.kfft_gb300_queue_selftest(1 << 12, 1) == 0
+        assert L.L.kfft_gb300_queue_selftest(1 << 12, 0) == 1
+        assert L.L.kfft_gb300_queue_selftest(1 << 12, 1) == 0  # still usable
+    x = np.arange(64, dtype=np.complex128)
+    assert rel_l2(lib.fft_cpx(x), O.fft_cpx(x)) <= 1e-13 * 6
