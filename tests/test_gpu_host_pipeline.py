@@ -87,3 +87,34 @@ def test_queue_wait_gives_up_and_reports(libf, lib):
         assert L.L.kfft_gb300_queue_selftest(1 << 12, 1) == 0  # still usable
     x = np.arange(64, dtype=np.complex128)
     assert rel_l2(lib.fft_cpx(x), O.fft_cpx(x)) <= 1e-13 * 6
+
+
+@pytest.mark.parametrize("logn", list(range(4, 13)) + [13, 16, 20, 22])
+def test_pipelined_power_of_two_passes(libf, logn):
+    """FP32 power-of-two passes run as resident CTAs that loop over many
+    tiles (2^22 points per call: more tiles than the GPU holds at once).
+    Forward and inverse against numpy's FP64 FFT, round trip, both directions
+    and in place."""
+    n = 1 << logn
+    batch = max(1, (1 << 22) // n)
+    rng = np.random.default_rng(logn)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    fwd = libf._plan("kfft_config_cpx", n, 0)
+    inv = libf._plan("kfft_config_cpx", n, K.FLAG_INVERSE)
+    try:
+        torch.cuda.synchronize()
+        assert libf.L.kfft_eval_cpx_async(fwd, xd.data_ptr(), yd.data_ptr(), batch, None) == 0
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy()
+        rows = sorted({0, batch // 2, batch - 1})
+        ref = np.fft.fft(x[rows].astype(np.complex128), axis=-1)
+        assert rel_l2(y[rows], ref) <= TOL32
+        # inverse in place on the device
+        assert libf.L.kfft_eval_cpx_async(inv, yd.data_ptr(), yd.data_ptr(), batch, None) == 0
+        torch.cuda.synchronize()
+        assert rel_l2(yd.cpu().numpy(), x) <= TOL32
+    finally:
+        libf.cleanup(fwd)
+        libf.cleanup(inv)
