@@ -472,6 +472,15 @@ bool cpx_init(kfft_plan_cpx* P, uint32_t nfft, uint32_t flags, kfft_pool_t* mm,
 
 }  // namespace
 
+namespace kfft {
+// The tuned plan variant of (nfft, flags) for planners outside this file (the
+// uneven batch), or -1 when none is recorded or it is not allowed.
+int tuned_plan_variant(uint32_t nfft, uint32_t flags) {
+    const int v = tuned_variant(nfft, flags);
+    return (v >= 0 && variant_allowed(uint32_t(v), flags)) ? v : -1;
+}
+}  // namespace kfft
+
 // ===========================================================================
 // complex 1D (kfft_cpx.c:315-366)
 // ===========================================================================

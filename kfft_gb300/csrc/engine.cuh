@@ -184,6 +184,8 @@ struct PlanVariant {
 };
 constexpr uint32_t kPlanVariants = 6;
 PlanVariant plan_variant(uint32_t index);
+// the variant the tuning table records for (nfft, flags), -1 if none
+int tuned_plan_variant(uint32_t nfft, uint32_t flags);
 
 struct FftPlan {
     uint32_t N = 0;

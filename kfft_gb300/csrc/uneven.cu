@@ -286,7 +286,12 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
         const uint32_t n = lengths[i];
         if (n == 0) continue;
         if (!P->plans.count(n)) {
-            FftPlan* fp = make_plan(n, sign, P->arena, st, kUnevenMaxPrime);
+            // a tuned variant is used when it keeps every pass in register
+            // tiles (the queue kernel's only tile kind); the record step checks
+            const int tv = tuned_plan_variant(n, flags);
+            PlanVariant var = tv >= 0 ? plan_variant(uint32_t(tv)) : PlanVariant();
+            if (var.no_fused) var = PlanVariant();
+            FftPlan* fp = make_plan(n, sign, P->arena, st, kUnevenMaxPrime, var);
             if (!fp) return NULL;
             P->plans[n].reset(fp);
         }

@@ -226,3 +226,28 @@ def test_small_tuning_run_reports_regret(libf, tmp_path):
     finally:
         model.close()
         libf.L.kfft_tune_clear()
+
+
+def test_uneven_batch_uses_tuned_variants(libf):
+    """The uneven-batch planner takes the tuning table's variant per length
+    (when it keeps register tiles); results stay within the FP32 bound."""
+    lengths = np.ascontiguousarray(np.array([1 << 18, 1 << 20, 3 << 16, 1000], dtype=np.uint32))
+    rng = np.random.default_rng(31)
+    total = int(lengths.sum())
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    L = libf.L
+    try:
+        assert L.kfft_tune_set(1 << 18, 0, 2) == 0
+        assert L.kfft_tune_set(1 << 20, 0, 1) == 0
+        assert L.kfft_tune_set(1000, 0, 3) == 0  # shared-memory tiles: not used by the queue
+        p = L.kfft_config_cpx_uneven(len(lengths), lengths.ctypes.data, 0)
+        assert p, libf.last_error()
+        y = np.empty_like(x)
+        assert L.kfft_eval_cpx_uneven(p, x.ctypes.data, y.ctypes.data) == 0
+        L.kfft_release_uneven(p)
+        offs = np.concatenate([[0], np.cumsum(lengths.astype(np.int64))])
+        for i in range(len(lengths)):
+            a, b = offs[i], offs[i + 1]
+            assert rel_l2(y[a:b], O.fft_cpx(x[a:b])) <= TOL32, int(lengths[i])
+    finally:
+        L.kfft_tune_clear()
