@@ -187,6 +187,9 @@ static std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
 // 30% more per point than radix-2/4/8/16 ones on this kernel; the nearest
 // 7-smooth length is often odd-heavy or one pass deeper than a power-of-two
 // one slightly above it.
+#ifndef KFFT_BLUESTEIN_ODD_COST
+#define KFFT_BLUESTEIN_ODD_COST 0.15
+#endif
 static uint64_t bluestein_length(uint64_t m) {
     uint64_t best = next_smooth(m);
     double best_cost = -1.0;
@@ -203,7 +206,8 @@ static uint64_t bluestein_length(uint64_t m) {
                             ++odd;
                         }
                     const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), kMultiRmax).size());
-                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) * (1.0 + 0.15 * odd);
+                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) *
+                                        (1.0 + KFFT_BLUESTEIN_ODD_COST * odd);
                     if (best_cost < 0 || cost < best_cost) {
                         best_cost = cost;
                         best = d;
