@@ -215,6 +215,196 @@ class Uniform(Workload):
         return self.flops_per_step() * n_done / el / 1e9, f"{n_done} steps of the full workload"
 
 
+class Config4(Workload):
+    """BASELINE config 4 shapes through the synchronous C ABI (device buffers
+    for `value`, pinned host buffers for `e2e`); one step = forward + inverse
+    (real, 2D) or one circular 2D convolution.  These entry points queue on
+    the calling thread's stream, so the bench times them there."""
+
+    timing_stream_ptr = 2  # cudaStreamPerThread
+
+    def __init__(self, lib, kind, precision, seed):
+        self.lib, self.kind, self.precision, self.seed = lib, kind, precision, seed
+        tag = "fp64" if precision == "double" else "fp32"
+        if kind == "real":
+            self.N, self.B = 1 << 22, 64
+            self.name = f"real {tag} N=2^22 batch 64 forward+inverse, U[-1,1)"
+        elif kind == "c2d":
+            self.X = self.Y = 8192 if precision == "float" else 4096
+            self.name = f"2D complex {tag} {self.X}x{self.Y} forward+inverse, N(0,1)"
+        else:
+            # image 4096^2 U[0,1) and a 63x63 Gaussian (sigma 8, sum 1), both
+            # zero-padded to M >= 4096 + 63 - 1 = 4158 for a linear convolution
+            self.M = 4160
+            self.name = (f"conv2d {tag} image 4096^2 U[0,1) * Gaussian 63x63 sigma 8, "
+                         f"zero-padded to {self.M}^2 (circular conv of padded arrays)")
+
+    def _real_t(self):
+        return np.float32 if self.precision == "float" else np.float64
+
+    def _cpx_t(self):
+        return np.complex64 if self.precision == "float" else np.complex128
+
+    def setup(self, torch, dev, nbuf):
+        rng = np.random.default_rng(self.seed)
+        L = self.lib.L
+        if self.kind == "real":
+            x = rng.uniform(-1, 1, (self.B, self.N)).astype(self._real_t())
+            self.host_in = x
+            self.fwd = L.kfft_config_scalar(self.N, 0, None, None)
+            self.inv = L.kfft_config_scalar(self.N, 1, None, None)
+            bins = self.N // 2 + 1
+            self.ins = [torch.from_numpy(x).to(dev)]
+            self.mid = torch.empty((self.B, bins), dtype=torch.complex64 if self.precision == "float"
+                                   else torch.complex128, device=dev)
+            self.out = torch.empty_like(self.ins[0])
+            self.pin_in = torch.from_numpy(x).pin_memory()
+            self.pin_mid = torch.empty(tuple(self.mid.shape), dtype=self.mid.dtype).pin_memory()
+            self.pin_out = torch.empty_like(self.pin_in).pin_memory()
+        elif self.kind == "c2d":
+            shape = (self.Y, self.X)
+            x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(self._cpx_t())
+            self.host_in = x
+            self.fwd = L.kfft_config2_cpx(self.X, self.Y, 0, None, None)
+            self.inv = L.kfft_config2_cpx(self.X, self.Y, 1, None, None)
+            self.ins = [torch.from_numpy(x).to(dev)]
+            self.mid = torch.empty_like(self.ins[0])
+            self.out = torch.empty_like(self.ins[0])
+            self.pin_in = torch.from_numpy(x).pin_memory()
+            self.pin_mid = torch.empty_like(self.pin_in).pin_memory()
+            self.pin_out = torch.empty_like(self.pin_in).pin_memory()
+        else:
+            M = self.M
+            img = np.zeros((M, M), self._real_t())
+            img[:4096, :4096] = rng.uniform(0, 1, (4096, 4096))
+            g = np.arange(63) - 31
+            k = np.exp(-(g[:, None] ** 2 + g[None, :] ** 2) / (2 * 8.0 ** 2))
+            ker = np.zeros((M, M), self._real_t())
+            ker[:63, :63] = k / k.sum()
+            self.host_in, self.host_ker = img, ker
+            self.plan = L.kfft_config2_conv_scalar(M, M, 0, None, None)
+            self.ins = [torch.from_numpy(img).to(dev)]
+            self.ker = torch.from_numpy(ker).to(dev)
+            self.out = torch.empty_like(self.ins[0])
+            self.pin_in = torch.from_numpy(img).pin_memory()
+            self.pin_ker = torch.from_numpy(ker).pin_memory()
+            self.pin_out = torch.empty_like(self.pin_in).pin_memory()
+        for p in ("fwd", "inv", "plan"):
+            if hasattr(self, p):
+                assert getattr(self, p), self.lib.last_error()
+
+    def elem_bytes(self):
+        return 4 if self.precision == "float" else 8  # one real value
+
+    def flops_per_step(self):
+        if self.kind == "real":
+            return 2 * 2.5 * self.N * math.log2(self.N) * self.B
+        if self.kind == "c2d":
+            n = self.X * self.Y
+            return 2 * 5.0 * n * math.log2(n)
+        n = self.M * self.M
+        return 3 * 2.5 * n * math.log2(n)  # two forward and one inverse real 2D transforms
+
+    def algorithmic_bytes_per_step(self):
+        s = self.elem_bytes()
+        if self.kind == "real":
+            return 2 * self.B * (self.N * s + (self.N // 2 + 1) * 2 * s)
+        if self.kind == "c2d":
+            return 2 * 2 * self.X * self.Y * 2 * s
+        return 3 * self.M * self.M * s  # two images read, one written
+
+    def step(self, i, stream):
+        L = self.lib.L
+        if self.kind == "real":
+            r1 = L.kfft_eval_scalar_batch(self.fwd, self.ins[0].data_ptr(), self.mid.data_ptr(), self.B)
+            r2 = L.kfft_evali_scalar_batch(self.inv, self.mid.data_ptr(), self.out.data_ptr(), self.B)
+        elif self.kind == "c2d":
+            r1 = L.kfft_eval2_cpx(self.fwd, self.ins[0].data_ptr(), self.mid.data_ptr())
+            r2 = L.kfft_eval2_cpx(self.inv, self.mid.data_ptr(), self.out.data_ptr())
+        else:
+            r1 = L.kfft_eval2_conv_scalar(self.plan, self.ins[0].data_ptr(), self.ker.data_ptr(),
+                                          self.out.data_ptr())
+            r2 = 0
+        assert r1 == 0 and r2 == 0, self.lib.last_error()
+
+    def step_e2e(self):
+        L = self.lib.L
+        if self.kind == "real":
+            r1 = L.kfft_eval_scalar_batch(self.fwd, self.pin_in.data_ptr(), self.pin_mid.data_ptr(), self.B)
+            r2 = L.kfft_evali_scalar_batch(self.inv, self.pin_mid.data_ptr(), self.pin_out.data_ptr(), self.B)
+        elif self.kind == "c2d":
+            r1 = L.kfft_eval2_cpx(self.fwd, self.pin_in.data_ptr(), self.pin_mid.data_ptr())
+            r2 = L.kfft_eval2_cpx(self.inv, self.pin_mid.data_ptr(), self.pin_out.data_ptr())
+        else:
+            r1 = L.kfft_eval2_conv_scalar(self.plan, self.pin_in.data_ptr(), self.pin_ker.data_ptr(),
+                                          self.pin_out.data_ptr())
+            r2 = 0
+        assert r1 == 0 and r2 == 0
+
+    def e2e_bytes(self):
+        if self.kind == "real":
+            a = self.pin_in.numel() * self.elem_bytes()
+            b = self.pin_mid.numel() * 2 * self.elem_bytes()
+            return a + b, a + b
+        if self.kind == "c2d":
+            a = self.pin_in.numel() * 2 * self.elem_bytes()
+            return 2 * a, 2 * a
+        a = self.pin_in.numel() * self.elem_bytes()
+        return 2 * a, a
+
+    def accuracy(self, oracle_mod):
+        """rel-L2 of the forward result against numpy's FP64 FFT on the same input."""
+        L = self.lib.L
+        if self.kind == "real":
+            x = np.ascontiguousarray(self.host_in[:2])
+            y = np.zeros((2, self.N // 2 + 1), self._cpx_t())
+            assert L.kfft_eval_scalar_batch(self.fwd, x.ctypes.data, y.ctypes.data, 2) == 0
+            ref = np.fft.rfft(x.astype(np.float64), axis=-1)
+        elif self.kind == "c2d":
+            x = self.host_in
+            y = np.empty_like(x)
+            assert L.kfft_eval2_cpx(self.fwd, x.ctypes.data, y.ctypes.data) == 0
+            ref = np.fft.fft2(x.astype(np.complex128))
+        else:
+            y = np.empty_like(self.host_in)
+            assert L.kfft_eval2_conv_scalar(self.plan, self.host_in.ctypes.data,
+                                            self.host_ker.ctypes.data, y.ctypes.data) == 0
+            a = self.host_in.astype(np.float64)
+            b = self.host_ker.astype(np.float64)
+            # the reference's even-length real inverse returns twice the input
+            ref = 2.0 * np.fft.irfft2(np.fft.rfft2(a) * np.fft.rfft2(b), s=a.shape)
+        return {"rel_l2_vs_fp64": float(np.linalg.norm(y - ref) / np.linalg.norm(ref)),
+                "reference": "numpy.fft (FP64, pocketfft) on the same input"}
+
+    def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
+        # bounded sample: the oracle's real / 2D / conv2d transforms in FP64
+        # on one host thread, repeated until the budget is spent
+        t0 = time.perf_counter()
+        calls, flops = 0, 0.0
+        while time.perf_counter() - t0 < budget_s:
+            if self.kind == "real":
+                X = oracle_mod.rfft(self.host_in[calls % self.B])
+                oracle_mod.irfft(X, self.N)
+                flops += 2 * 2.5 * self.N * math.log2(self.N)
+            elif self.kind == "c2d":
+                oracle_mod.fft2_cpx(self.host_in)
+                flops += 5.0 * self.X * self.Y * math.log2(self.X * self.Y)
+            else:
+                oracle_mod.conv2_scalar(self.host_in, self.host_ker)
+                flops += self.flops_per_step()
+            calls += 1
+        el = time.perf_counter() - t0
+        return flops / el / 1e9, f"{calls} oracle calls on one thread, {el:.1f}s"
+
+
+CONFIG4_WORKLOADS = {
+    "real_f32_2p22x64": lambda lib: Config4(lib, "real", "float", 5),
+    "c2d_f32_8192": lambda lib: Config4(lib, "c2d", "float", 6),
+    "c2d_f64_4096": lambda lib: Config4(lib, "c2d", "double", 6),
+    "conv2d_f32_4096": lambda lib: Config4(lib, "conv2d", "float", 7),
+}
+
+
 def C2C4096(lib):
     return Uniform(lib, 4096, 256, "double", 1, "uniform")
 
@@ -481,6 +671,8 @@ def run_learned_planner(args):
 def make_workload(name, lib, need_lib=True, subset=1, precision="float"):
     if name in UNIFORM_WORKLOADS:
         return UNIFORM_WORKLOADS[name](lib)
+    if name in CONFIG4_WORKLOADS:
+        return CONFIG4_WORKLOADS[name](lib)
     return Uneven(lib, precision=precision, subset=subset)
 
 
@@ -491,7 +683,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("KFFT_BENCH_WORKLOAD", "uneven"),
-                    choices=["uneven", "learned_planner"] + sorted(UNIFORM_WORKLOADS))
+                    choices=["uneven", "learned_planner"] + sorted(UNIFORM_WORKLOADS)
+                    + sorted(CONFIG4_WORKLOADS))
     ap.add_argument("--stride", type=int, default=1,
                     help="learned_planner: keep every k-th length of the sweep")
     ap.add_argument("--tune-db", default="",
@@ -530,6 +723,9 @@ def main():
         nbuf = max(1, int(math.ceil(268e6 / wl.bytes_per_buffer())))
     wl.setup(torch, dev, nbuf)
     stream = torch.cuda.Stream(device=dev)
+    if getattr(wl, "timing_stream_ptr", None) is not None:
+        # synchronous entry points queue on the thread's own stream: time there
+        stream = torch.cuda.ExternalStream(wl.timing_stream_ptr, device=dev)
     sptr = stream.cuda_stream
 
     with torch.cuda.stream(stream):
@@ -621,6 +817,14 @@ def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_ste
     """Roofline of the dominant kernel: algorithmic bytes of one launch (read +
     write every point it transforms once) over the average launch time."""
     es = 8 if wl.precision == "float" else 16
+    if isinstance(wl, Config4):
+        # several kernels per step (passes, real pre/post, transposes,
+        # spectrum product): the algorithmic bytes of the step over its time
+        achieved = wl.algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "kernel": "all launches of the step (per step, not per launch)",
+                "launches_per_step": launches_per_step}
     if hasattr(wl, "algorithmic_bytes_per_step"):
         # uniform batches: every pass launch reads and writes every point once
         n = max(1, int(round(launches_per_step or 1)))
