@@ -325,7 +325,7 @@ class Config4(Workload):
             r1 = L.kfft_eval2_conv_scalar(self.plan, self.ins[0].data_ptr(), self.ker.data_ptr(),
                                           self.out.data_ptr())
             r2 = 0
-        assert r1 == 0 and r2 == 0, self.lib.last_error()
+        assert r1 == 0 and r2 == 0, (r1, r2, self.lib.last_error())
 
     def step_e2e(self):
         L = self.lib.L

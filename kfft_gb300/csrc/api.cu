@@ -783,7 +783,7 @@ KFFT_API kfft_return_t kfft_eval_scalar_batch(kfft_plan_sclr* plan, const kfft_s
     Carve cv;
     cv.base = static_cast<char*>(g->workspace(need));
     cv.size = need;
-    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;  // nothing to carve: no buffer needed
     const real_t* din = reinterpret_cast<const real_t*>(fin);
     vec2_t* dout = reinterpret_cast<vec2_t*>(fout);
     if (hin) {
@@ -821,7 +821,7 @@ KFFT_API kfft_return_t kfft_evali_scalar_batch(kfft_plan_sclr* plan, const kfft_
     Carve cv;
     cv.base = static_cast<char*>(g->workspace(need));
     cv.size = need;
-    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;  // nothing to carve: no buffer needed
     const vec2_t* din = reinterpret_cast<const vec2_t*>(fin);
     real_t* dout = reinterpret_cast<real_t*>(fout);
     if (hin) {
@@ -989,7 +989,7 @@ kfft_return_t with_staging(kfft_gpu_plan* g, size_t work, const void* const* ins
     Carve cv;
     cv.base = static_cast<char*>(g->workspace(need));
     cv.size = need;
-    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;  // nothing to carve: no buffer needed
     const void* dins[4];
     for (int i = 0; i < nin; ++i) {
         if (hin[i]) {

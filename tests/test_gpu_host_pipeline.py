@@ -118,3 +118,28 @@ def test_pipelined_power_of_two_passes(libf, logn):
     finally:
         libf.cleanup(fwd)
         libf.cleanup(inv)
+
+
+def test_device_buffers_on_a_fresh_plan_need_no_workspace(lib, libf):
+    """A fresh 2D or real plan whose passes need no scratch, called first with
+    device buffers (nothing to stage), runs instead of failing for want of a
+    workspace allocation of zero bytes."""
+    for L, cdt, rdt, tol in ((lib, torch.complex128, torch.float64, 1e-13 * 12),
+                             (libf, torch.complex64, torch.float32, TOL32)):
+        rng = np.random.default_rng(5)
+        a = rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64))
+        p = L.L.kfft_config2_cpx(64, 64, 0, None, None)
+        ad = torch.from_numpy(a.astype(L.cpx)).cuda()
+        od = torch.empty_like(ad)
+        torch.cuda.synchronize()
+        assert L.L.kfft_eval2_cpx(p, ad.data_ptr(), od.data_ptr()) == 0, L.last_error()
+        assert rel_l2(od.cpu().numpy(), np.fft.fft2(a)) <= tol
+        L.cleanup(p)
+        x = rng.standard_normal(4096)
+        p = L.L.kfft_config_scalar(4096, 0, None, None)
+        xd = torch.from_numpy(x.astype(L.real)).cuda()
+        yd = torch.empty(2049, dtype=cdt, device="cuda")
+        torch.cuda.synchronize()
+        assert L.L.kfft_eval_scalar(p, xd.data_ptr(), yd.data_ptr()) == 0, L.last_error()
+        assert rel_l2(yd.cpu().numpy(), np.fft.rfft(x)) <= tol
+        L.cleanup(p)
