@@ -377,8 +377,9 @@ class Config4(Workload):
                 "reference": "numpy.fft (FP64, pocketfft) on the same input"}
 
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
-        # bounded sample: the oracle's real / 2D / conv2d transforms in FP64
-        # on one host thread, repeated until the budget is spent
+        # bounded sample: the oracle's real / 2D / conv2d transforms in FP64,
+        # repeated until the budget is spent (the 2D ones run their row and
+        # column loops over all host threads, the 1D real one on one thread)
         t0 = time.perf_counter()
         calls, flops = 0, 0.0
         while time.perf_counter() - t0 < budget_s:
@@ -394,7 +395,8 @@ class Config4(Workload):
                 flops += self.flops_per_step()
             calls += 1
         el = time.perf_counter() - t0
-        return flops / el / 1e9, f"{calls} oracle calls on one thread, {el:.1f}s"
+        how = "one thread" if self.kind == "real" else "OpenMP over rows and columns"
+        return flops / el / 1e9, f"{calls} oracle calls ({how}), {el:.1f}s"
 
 
 CONFIG4_WORKLOADS = {
