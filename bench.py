@@ -396,7 +396,8 @@ class Config4(Workload):
             calls += 1
         el = time.perf_counter() - t0
         how = "one thread" if self.kind == "real" else "OpenMP over rows and columns"
-        return flops / el / 1e9, f"{calls} oracle calls ({how}), {el:.1f}s"
+        cores = 1 if self.kind == "real" else threads
+        return flops / el / 1e9, f"{calls} oracle calls ({how}), {el:.1f}s", cores
 
 
 CONFIG4_WORKLOADS = {
@@ -785,8 +786,10 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
         threads = os.cpu_count() or 1
-        v, sample = wl.cpu_sample(oracle, threads)
-        line["cpu_baseline"] = {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads,
+        res = wl.cpu_sample(oracle, threads)
+        v, sample = res[0], res[1]
+        cores = res[2] if len(res) > 2 else threads  # the threads the sample really used
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "GFLOP/s", "cores": cores,
                                 "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
