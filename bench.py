@@ -216,7 +216,7 @@ class Uniform(Workload):
 
 
 class Config4(Workload):
-    """BASELINE config 4 shapes through the synchronous C ABI (device buffers
+    """Real, 2D and 2D-convolution shapes through the synchronous C ABI (device buffers
     for `value`, pinned host buffers for `e2e`); one step = forward + inverse
     (real, 2D) or one circular 2D convolution.  These entry points queue on
     the calling thread's stream, so the bench times them there."""

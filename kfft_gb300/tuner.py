@@ -9,8 +9,8 @@ This module chooses between them.
 
 * ``exhaustive`` times every distinct variant of every length on the GPU (CUDA
   events on the launching stream, device-resident buffers, median of a few
-  launches) and returns the records.  It is the fallback and the judge of the
-  learned model.
+  launches) and returns the records.  It is the fallback of the learned model
+  and the yardstick its regret is measured against.
 * ``CostModel`` is a 3-layer 64-wide MLP trained by the engine's own CUDA
   kernels (``kfft_mlp_train``) on the log launch time of (length, variant)
   records.  Features: log2 N, log2 batch, precision, the exponents of the
