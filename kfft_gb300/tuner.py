@@ -67,7 +67,9 @@ def inner_length(n: int, max_prime: int = MAX_DIRECT_PRIME) -> int:
 
     Follows the engine's planner: a length whose prime factors are all at most
     ``max_prime`` is direct; a prime whose p-1 is direct runs Rader on p-1;
-    anything else runs Bluestein on the smallest 7-smooth M >= 2n-1.
+    anything else runs Bluestein on a 7-smooth M >= 2n-1.  The feature uses
+    the smallest such M; the planner may take a slightly longer one that needs
+    fewer or cheaper passes, which changes the feature's scale very little.
     """
     def direct(m):
         return m <= 1 or all(q <= max_prime for q in factorize(m))
