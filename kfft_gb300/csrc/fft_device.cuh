@@ -1149,7 +1149,9 @@ __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const I
 // two shared-memory round trips fewer than tile_body.  Shared memory holds two
 // buffers of pad(C*R)+1 elements (only when the sub-FFT has 3+ inner passes;
 // one buffer for 2 passes; none for 1).
-template <bool INV>
+// SPEC: dispatch power-of-two passes (d.spec) to their compile-time bodies;
+// the pass kernel launches those as kernels of their own and leaves it off.
+template <bool INV, bool SPEC = true>
 __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra& x, uint32_t tile,
                                               vec2_t* sm) {
     const uint32_t total = d.batch * d.lanes_j;
@@ -1174,7 +1176,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     vec2_t* bufA = sm;
     vec2_t* bufB = sm + pad(d.C * d.R) + 1;
 #if defined(KFFT_HALF_SCALAR)
-    switch (d.spec) {
+    if constexpr (SPEC) switch (d.spec) {
         case 4: tile_body_spec<16, INV>(d, lane0, total, bufA, bufB); return;
         case 5: tile_body_spec<32, INV>(d, lane0, total, bufA, bufB); return;
         case 6: tile_body_spec<64, INV>(d, lane0, total, bufA, bufB); return;

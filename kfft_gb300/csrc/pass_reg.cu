@@ -1,6 +1,7 @@
 // pass_reg.cu -- the register-resident pass kernel k_pass_reg.
 #include "fft_device.cuh"
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -11,48 +12,80 @@ template <bool INV>
 __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_pass_reg(const __grid_constant__ PassDesc d,
                                                               const __grid_constant__ PassExtra x) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    tile_body_reg<INV>(d, x, blockIdx.x, reinterpret_cast<vec2_t*>(smem_raw));
+    // power-of-two FP32 passes launch k_pass_spec / k_pass_pipe instead
+    tile_body_reg<INV, false>(d, x, blockIdx.x, reinterpret_cast<vec2_t*>(smem_raw));
 }
 
 #if defined(KFFT_HALF_SCALAR)
-// FP32 power-of-two passes with a plain prologue and more tiles than fit the
-// GPU at once: a grid of resident CTAs, each running many tiles with its next
-// tile's loads in flight (tile_loop_pipelined).  The FP64 build does not use
-// it: the FP64 pipe, not load latency, bounds that path, and the second tile's
-// registers would spill.
-template <bool INV>
+// FP32 power-of-two passes, one kernel per pass length R so each kernel holds
+// only its own body (a small instruction footprint):
+// * k_pass_pipe: a plain prologue and more tiles than fit the GPU at once: a
+//   grid of resident CTAs, each running many tiles with its next tile's loads
+//   in flight (tile_loop_pipelined);
+// * k_pass_spec: one tile per CTA otherwise.
+// The FP64 build uses neither: the FP64 pipe, not index arithmetic or load
+// latency, bounds that path, and its unrolled bodies would spill.
+template <uint32_t R, bool INV>
 __global__ void __launch_bounds__(kPassThreads, 2) k_pass_pipe(const __grid_constant__ PassDesc d) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    vec2_t* sm = reinterpret_cast<vec2_t*>(smem_raw);
-    switch (d.spec) {
-        case 4: tile_loop_pipelined<16, INV>(d, sm); break;
-        case 5: tile_loop_pipelined<32, INV>(d, sm); break;
-        case 6: tile_loop_pipelined<64, INV>(d, sm); break;
-        case 7: tile_loop_pipelined<128, INV>(d, sm); break;
-        case 8: tile_loop_pipelined<256, INV>(d, sm); break;
-        case 9: tile_loop_pipelined<512, INV>(d, sm); break;
-        case 10: tile_loop_pipelined<1024, INV>(d, sm); break;
-        case 11: tile_loop_pipelined<2048, INV>(d, sm); break;
-        case 12: tile_loop_pipelined<4096, INV>(d, sm); break;
-        default: break;
-    }
+    tile_loop_pipelined<R, INV>(d, reinterpret_cast<vec2_t*>(smem_raw));
 }
 
+template <uint32_t R, bool INV>
+__global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_pass_spec(
+    const __grid_constant__ PassDesc d) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    vec2_t* sm = reinterpret_cast<vec2_t*>(smem_raw);
+    tile_body_spec<R, INV>(d, blockIdx.x * d.C, d.batch * d.lanes_j, sm, sm + pad(d.C * R) + 1);
+}
+
+using SpecKernel = void (*)(PassDesc);
+
+template <uint32_t R>
+SpecKernel pick(bool pipe, bool inv) {
+    if (pipe) return inv ? k_pass_pipe<R, true> : k_pass_pipe<R, false>;
+    return inv ? k_pass_spec<R, true> : k_pass_spec<R, false>;
+}
+
+SpecKernel spec_kernel(uint32_t spec, bool pipe, bool inv) {
+    switch (spec) {
+        case 4: return pick<16>(pipe, inv);
+        case 5: return pick<32>(pipe, inv);
+        case 6: return pick<64>(pipe, inv);
+        case 7: return pick<128>(pipe, inv);
+        case 8: return pick<256>(pipe, inv);
+        case 9: return pick<512>(pipe, inv);
+        case 10: return pick<1024>(pipe, inv);
+        case 11: return pick<2048>(pipe, inv);
+        case 12: return pick<4096>(pipe, inv);
+        default: return nullptr;
+    }
+}
 #endif
 
 namespace {
 #if defined(KFFT_HALF_SCALAR)
-// resident CTAs per SM of k_pass_pipe for a dynamic shared-memory size
-int pipe_blocks_per_sm(bool inv, uint32_t smem) {
+// Raises the dynamic shared-memory limit of a kernel once and caches its
+// resident CTAs per SM for a shared-memory size.
+int prepare(SpecKernel f, uint32_t smem) {
     static std::mutex mu;
-    static std::map<std::pair<bool, uint32_t>, int> cache;
+    static std::map<std::pair<SpecKernel, uint32_t>, int> cache;
+    static std::map<SpecKernel, bool> configured;
     std::lock_guard<std::mutex> lk(mu);
-    auto key = std::make_pair(inv, smem);
+    if (!configured[f]) {
+        if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 227 * 1024) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        configured[f] = true;
+    }
+    auto key = std::make_pair(f, smem);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     int n = 0;
-    const void* f = inv ? (const void*)k_pass_pipe<true> : (const void*)k_pass_pipe<false>;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kPassThreads, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)f, kPassThreads, smem) !=
+        cudaSuccess) {
         cudaGetLastError();
         n = 0;
     }
@@ -87,24 +120,22 @@ void launch_pass_reg(const PassDesc& d, const PassExtra& x, cudaStream_t st) {
         configured = true;
     }
 #if defined(KFFT_HALF_SCALAR)
-    static bool pipe_configured = false;
-    if (!pipe_configured) {
-        for (const void* f : {(const void*)k_pass_pipe<false>, (const void*)k_pass_pipe<true>}) {
-            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 227 * 1024);
-            if (e != cudaSuccess) {
-                note_cuda_error(e);
+    if (d.spec && d.threads == kPassThreads) {
+        const bool inv = d.inv != 0;
+        if (d.pro_op == PRO_NONE) {
+            SpecKernel f = spec_kernel(d.spec, true, inv);
+            const int per_sm = f ? prepare(f, d.smem_bytes) : -1;
+            const uint32_t grid = uint32_t(std::max(per_sm, 0)) * uint32_t(sm_count());
+            if (per_sm > 0 && d.tiles >= 2 * grid) {
+                f<<<grid, kPassThreads, d.smem_bytes, st>>>(d);
+                note_cuda_error(cudaGetLastError());
+                count_launch();
                 return;
             }
         }
-        pipe_configured = true;
-    }
-    if (d.spec && d.pro_op == PRO_NONE && d.threads == kPassThreads) {
-        const int per_sm = pipe_blocks_per_sm(d.inv != 0, d.smem_bytes);
-        const uint32_t grid = uint32_t(per_sm) * uint32_t(sm_count());
-        if (per_sm > 0 && d.tiles >= 2 * grid) {
-            if (d.inv) k_pass_pipe<true><<<grid, kPassThreads, d.smem_bytes, st>>>(d);
-            else k_pass_pipe<false><<<grid, kPassThreads, d.smem_bytes, st>>>(d);
+        SpecKernel f = spec_kernel(d.spec, false, inv);
+        if (f && prepare(f, d.smem_bytes) > 0) {
+            f<<<d.tiles, kPassThreads, d.smem_bytes, st>>>(d);
             note_cuda_error(cudaGetLastError());
             count_launch();
             return;
