@@ -1151,7 +1151,9 @@ __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const I
 // one buffer for 2 passes; none for 1).
 // SPEC: dispatch power-of-two passes (d.spec) to their compile-time bodies;
 // the pass kernel launches those as kernels of their own and leaves it off.
-template <bool INV, bool SPEC = true>
+// TC: keep the tensor-core radix-16 stage; the queue kernel leaves it off
+// (its planner clears d.tc) to keep its instruction footprint small.
+template <bool INV, bool SPEC = true, bool TC = true>
 __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra& x, uint32_t tile,
                                               vec2_t* sm) {
     const uint32_t total = d.batch * d.lanes_j;
@@ -1192,7 +1194,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     const vec2_t* src = nullptr;
 #if defined(KFFT_HALF_SCALAR)
     TcFrag Fr, Fi, Gm;
-    if (d.tc) {
+    if (TC && d.tc) {
         Fr = dft16_frag<INV>(0);
         Fi = dft16_frag<INV>(1);
         Gm = dft16_frag<INV>(2);
@@ -1203,7 +1205,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
         vec2_t* dst = last ? nullptr : ((p % 2 == 0) ? bufA : bufB);
         const int sio = p == 0 ? IO_GLOBAL : IO_SMEM, dio = last ? IO_GLOBAL : IO_SMEM;
 #if defined(KFFT_HALF_SCALAR)
-        if (d.tc && d.rad[p] == 16)
+        if (TC && d.tc && d.rad[p] == 16)
             tc_pass16<INV>(d, x.step[p], src, dst, lane0, total, sio, dio, Fr, Fi, Gm);
         else
 #endif

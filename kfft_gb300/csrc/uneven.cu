@@ -124,8 +124,10 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
         }
     }
     const uint32_t nd = uint32_t(all.size());
-    for (const PassDesc& d : all)
+    for (PassDesc& d : all) {
         if (!d.regmode) return false;  // the queue kernel runs register-resident tiles only
+        d.tc = 0;  // and its radix-16 stages on CUDA cores (a smaller kernel)
+    }
     std::vector<Item> items;
     uint32_t smem = 0;
     for (uint32_t d = 0; d < nd; ++d) {
