@@ -283,10 +283,10 @@ CopyStreams* copy_streams() {
 // Number of chunks a host-buffer batch of `bytes` in `batch` sequences is
 // split into so that its copies overlap the transform (1: no split).
 uint32_t host_chunks(size_t bytes, uint32_t batch) {
-    constexpr size_t kChunkBytes = size_t(32) << 20;
-    if (batch < 2 || bytes < 2 * kChunkBytes) return 1;
+    constexpr size_t kChunkBytes = size_t(16) << 20;
+    if (batch < 2 || bytes < 4 * kChunkBytes) return 1;
     size_t k = bytes / kChunkBytes;
-    if (k > 8) k = 8;
+    if (k > 16) k = 16;
     if (k > batch) k = batch;
     return uint32_t(k);
 }

@@ -242,9 +242,9 @@ kfft_return_t launch(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2
 // Contiguous groups of about equal points for the host-buffer path: copies
 // of one group overlap the transform of its neighbours.
 void make_groups(kfft_plan_uneven* P) {
-    constexpr uint64_t kGroupPoints = uint64_t(1) << 24;
+    constexpr uint64_t kGroupPoints = uint64_t(1) << 23;
     const size_t count = P->lengths.size();
-    const uint64_t k = std::min<uint64_t>(8, P->total / kGroupPoints);
+    const uint64_t k = std::min<uint64_t>(16, P->total / kGroupPoints);
     if (k < 2 || count < 2) return;
     std::vector<std::pair<size_t, size_t>> ranges;
     size_t s = 0;
