@@ -834,8 +834,8 @@ def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, devi
 # (dram__bytes_read.sum + dram__bytes_write.sum).  The uneven batch is too
 # large for a full-set capture: every 8th sequence was captured (37.47 M
 # points, 2.099 GB) and scaled by points, which the same length mix allows.
-NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.094e9 / 37465227}
-NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.1e6, "c2c_f32_2p18x64": 219.4e6}
+NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.087e9 / 37465227}
+NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.3e6, "c2c_f32_2p18x64": 219.5e6}
 
 
 def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_step=None,
