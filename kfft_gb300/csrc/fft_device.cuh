@@ -1127,6 +1127,135 @@ __device__ __forceinline__ void tile_loop_pipelined(const PassDesc& d, vec2_t* s
     }
 }
 
+#if defined(KFFT_HALF_SCALAR)
+// ---------------------------------------------------------------------------
+// single-pass power-of-two tiles fed by the tensor memory accelerator: the
+// C sequences of a tile are C*R contiguous points, so one bulk copy
+// (cp.async.bulk, completion counted on an mbarrier) moves the next tile
+// into shared memory while the current one's later stages run.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return uint32_t(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+// one bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, its completion counted on `bar`
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// bounded wait for phase `parity` of `bar`; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n"
+            " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Shared memory: [mbarrier | pad to 128 B | raw tile C*R | bufA | bufB].
+// A wait that runs out (only a failed copy can cause it) ends the CTA after
+// recording the failure in *fail.
+template <uint32_t R, bool INV>
+__device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char* smem,
+                                               uint32_t* fail) {
+    constexpr uint32_t L = ilog2(R);
+    constexpr uint32_t K16 = L / 4;
+    constexpr int T = 1 << (L % 4);
+    constexpr int NP = int(K16) + (T > 1 ? 1 : 0);
+    constexpr int PL = T > 1 ? T : 16;
+    constexpr uint32_t M0 = R / 16;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    vec2_t* raw = reinterpret_cast<vec2_t*>(smem + 128);
+    vec2_t* bufA = raw + d.C * R;
+    vec2_t* bufB = bufA + pad(d.C * R) + 1;
+    const uint32_t total = d.batch;  // one lane per sequence (lanes_j == 1)
+    const uint32_t it = threadIdx.x;
+    const bool act = it < d.C * M0;
+    const uint32_t c0 = it / M0, jj0 = it % M0;
+    auto issue = [&](uint32_t tile) {
+        const uint32_t s0 = tile * d.C;
+        const uint32_t n = min(d.C, total - s0);
+        bulk_load(raw, d.in + uint64_t(s0) * d.in_bs, n * R * uint32_t(sizeof(vec2_t)), bar);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < d.tiles) issue(tile);
+    uint32_t parity = 0;
+    for (; tile < d.tiles; tile += gridDim.x) {
+        // every thread waits (the mbarrier's completion makes the copied data
+        // visible to it); the CTA leaves together if any wait ran out, after
+        // a second bounded wait that lets the copy in flight land first
+        const bool ok = mbar_wait(bar, parity);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(fail, 1u);
+            mbar_wait(bar, parity);
+            return;
+        }
+        parity ^= 1u;
+        const uint32_t lane0 = tile * d.C;
+        const uint32_t g = lane0 + c0;
+        const bool live = act && g < total;
+        vec2_t v[16];
+        if (live) {
+            const vec2_t* p0 = raw + c0 * R + jj0;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] = p0[q * M0];
+        }
+        __syncthreads();  // every read of raw is done: the next copy may land there
+        const uint32_t nt = tile + gridDim.x;
+        if (threadIdx.x == 0 && nt < d.tiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(nt);
+        }
+        if (act) {
+            if (!live) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = {0.f, 0.f};
+            }
+            dft<16, INV>(v);
+            const uint32_t ob = jj0 * 16;
+            if constexpr (NP == 1) {
+                if (live) fused_store<16>(d, g, 0, ob, 1, v);
+            } else {
+                vec2_t* p0 = bufA + pad(c0 * R + ob);  // 16 slots inside one pad period
+#pragma unroll
+                for (int q = 0; q < 16; ++q) p0[q] = v[q];
+            }
+        }
+        if constexpr (NP == 2) {
+            __syncthreads();
+            spec_stage<PL, R, 16, IO_SMEM, IO_GLOBAL, INV>(d, bufA, nullptr, lane0, total);
+        } else if constexpr (NP == 3) {
+            __syncthreads();
+            spec_stage<16, R, 16, IO_SMEM, IO_SMEM, INV>(d, bufA, bufB, lane0, total);
+            __syncthreads();
+            spec_stage<PL, R, 256, IO_SMEM, IO_GLOBAL, INV>(d, bufB, nullptr, lane0, total);
+        }
+        __syncthreads();  // the next tile's first stage overwrites bufA
+    }
+}
+#endif
+
 template <bool INV>
 __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
                                                const vec2_t* src, vec2_t* dst, uint32_t lane0,

@@ -39,25 +39,40 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_pass_spec(
     tile_body_spec<R, INV>(d, blockIdx.x * d.C, d.batch * d.lanes_j, sm, sm + pad(d.C * R) + 1);
 }
 
+// Set when a bulk-copy wait of k_pass_bulk ran out (only a failed copy can
+// cause it); the CTA then ends without finishing its tiles.
+__device__ uint32_t g_bulk_wait_failed = 0;
+
+// Single-pass FP32 power-of-two batches of contiguous sequences: each tile's
+// points arrive by one bulk copy (tile_loop_bulk).
+template <uint32_t R, bool INV>
+__global__ void __launch_bounds__(kPassThreads, 2) k_pass_bulk(const __grid_constant__ PassDesc d) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    tile_loop_bulk<R, INV>(d, smem_raw, &g_bulk_wait_failed);
+}
+
 using SpecKernel = void (*)(PassDesc);
 
+enum SpecKind { SPEC_ONE_TILE = 0, SPEC_PIPE = 1, SPEC_BULK = 2 };
+
 template <uint32_t R>
-SpecKernel pick(bool pipe, bool inv) {
-    if (pipe) return inv ? k_pass_pipe<R, true> : k_pass_pipe<R, false>;
+SpecKernel pick(int kind, bool inv) {
+    if (kind == SPEC_BULK) return inv ? k_pass_bulk<R, true> : k_pass_bulk<R, false>;
+    if (kind == SPEC_PIPE) return inv ? k_pass_pipe<R, true> : k_pass_pipe<R, false>;
     return inv ? k_pass_spec<R, true> : k_pass_spec<R, false>;
 }
 
-SpecKernel spec_kernel(uint32_t spec, bool pipe, bool inv) {
+SpecKernel spec_kernel(uint32_t spec, int kind, bool inv) {
     switch (spec) {
-        case 4: return pick<16>(pipe, inv);
-        case 5: return pick<32>(pipe, inv);
-        case 6: return pick<64>(pipe, inv);
-        case 7: return pick<128>(pipe, inv);
-        case 8: return pick<256>(pipe, inv);
-        case 9: return pick<512>(pipe, inv);
-        case 10: return pick<1024>(pipe, inv);
-        case 11: return pick<2048>(pipe, inv);
-        case 12: return pick<4096>(pipe, inv);
+        case 4: return pick<16>(kind, inv);
+        case 5: return pick<32>(kind, inv);
+        case 6: return pick<64>(kind, inv);
+        case 7: return pick<128>(kind, inv);
+        case 8: return pick<256>(kind, inv);
+        case 9: return pick<512>(kind, inv);
+        case 10: return pick<1024>(kind, inv);
+        case 11: return pick<2048>(kind, inv);
+        case 12: return pick<4096>(kind, inv);
         default: return nullptr;
     }
 }
@@ -122,8 +137,24 @@ void launch_pass_reg(const PassDesc& d, const PassExtra& x, cudaStream_t st) {
 #if defined(KFFT_HALF_SCALAR)
     if (d.spec && d.threads == kPassThreads) {
         const bool inv = d.inv != 0;
+        // one pass over whole contiguous sequences, 16-byte aligned: the
+        // tiles arrive by bulk copy
+        const bool contiguous = d.lanes_j == 1 && d.order == ORDER_J && d.in_es == 1 &&
+                                d.in_bs == d.R && (reinterpret_cast<uintptr_t>(d.in) & 15u) == 0;
+        if (d.pro_op == PRO_NONE && contiguous) {
+            SpecKernel f = spec_kernel(d.spec, SPEC_BULK, inv);
+            const uint32_t smem = 128 + d.C * d.R * uint32_t(sizeof(vec2_t)) + d.smem_bytes;
+            const int per_sm = f ? prepare(f, smem) : -1;
+            const uint32_t grid = uint32_t(std::max(per_sm, 0)) * uint32_t(sm_count());
+            if (per_sm > 0 && d.tiles >= 2 * grid) {
+                f<<<grid, kPassThreads, smem, st>>>(d);
+                note_cuda_error(cudaGetLastError());
+                count_launch();
+                return;
+            }
+        }
         if (d.pro_op == PRO_NONE) {
-            SpecKernel f = spec_kernel(d.spec, true, inv);
+            SpecKernel f = spec_kernel(d.spec, SPEC_PIPE, inv);
             const int per_sm = f ? prepare(f, d.smem_bytes) : -1;
             const uint32_t grid = uint32_t(std::max(per_sm, 0)) * uint32_t(sm_count());
             if (per_sm > 0 && d.tiles >= 2 * grid) {
@@ -133,7 +164,7 @@ void launch_pass_reg(const PassDesc& d, const PassExtra& x, cudaStream_t st) {
                 return;
             }
         }
-        SpecKernel f = spec_kernel(d.spec, false, inv);
+        SpecKernel f = spec_kernel(d.spec, SPEC_ONE_TILE, inv);
         if (f && prepare(f, d.smem_bytes) > 0) {
             f<<<d.tiles, kPassThreads, d.smem_bytes, st>>>(d);
             note_cuda_error(cudaGetLastError());

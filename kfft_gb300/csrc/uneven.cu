@@ -411,14 +411,14 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_c
         if (hout) cudaMemcpyAsync(fout, dout, bytes, cudaMemcpyDeviceToHost, st);
     }
     // the queue kernel's error word: set when a dependency wait gave up
+    std::vector<uint32_t> words(used.size(), 0);
+    for (size_t i = 0; i < used.size(); ++i)
+        cudaMemcpyAsync(&words[i], used[i]->counters + 1, sizeof(uint32_t),
+                        cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) note_cuda_error(e);
     uint32_t err = 0;
-    for (UnevenQueue* Q : used) {
-        uint32_t e1 = 0;
-        cudaMemcpyAsync(&e1, Q->counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-        cudaError_t e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) note_cuda_error(e);
-        err |= e1;
-    }
+    for (uint32_t w : words) err |= w;
     if (take_pending_error() || err) return KFFT_RET_BUFFER_FAIL;
     return KFFT_RET_SUCCESS;
 }
