@@ -491,6 +491,29 @@ class Uneven(Workload):
         b = self.total * (8 if self.precision == "float" else 16)
         return b, b
 
+    def accuracy(self, oracle_mod):
+        """rel-L2 against an FP64 FFT (numpy's: fast for any prime) on the
+        longest sequence of each kind (direct, Rader, Bluestein), and the
+        worst over them."""
+        x = self.pin_in.numpy()
+        y = self.pin_out.numpy()  # the last e2e step's output of this input
+        offs = np.concatenate([[0], np.cumsum(self.lengths.astype(np.int64))])
+        import kfft_gb300.tuner as T
+        picks = {}
+        for i, n in enumerate(self.lengths.tolist()):
+            inner = T.inner_length(n, max_prime=13)
+            kind = "direct" if inner == 0 else ("rader" if inner == n - 1 else "bluestein")
+            if kind not in picks or n > self.lengths[picks[kind]]:
+                picks[kind] = i
+        out = {}
+        for kind, i in picks.items():
+            a, b = offs[i], offs[i + 1]
+            ref = np.fft.fft(x[a:b].astype(np.complex128))
+            out[f"{kind}_N{int(self.lengths[i])}"] = float(np.linalg.norm(y[a:b] - ref) / np.linalg.norm(ref))
+        out["worst"] = max(out.values())
+        out["against"] = "numpy.fft in FP64, longest sequence of each kind"
+        return out
+
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
         # bounded sample: every 16th sequence of the batch, all host threads,
         # OpenMP over sequences; repeated until the budget is spent
