@@ -39,6 +39,9 @@ constexpr uint32_t kPassThreads = 256;
 // the first inner pass reads global memory, the last writes it, and the
 // passes between exchange through two shared-memory buffers.
 constexpr uint32_t kRegTile = 4096;
+// Slots added after every lane of a compile-time (power-of-two) tile in
+// shared memory, so that lane-major accesses spread over the banks.
+constexpr uint32_t kLaneSkew = 4;
 // Largest prime factor a DIRECT plan accepts; larger primes go to Rader/Bluestein.
 constexpr uint32_t kMaxDirectPrime = 31;
 

@@ -605,7 +605,9 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     if (d.regmode) {
         d.threads = kPassThreads;
         const uint32_t nbuf = s.radices.size() >= 3 ? 2u : (s.radices.size() == 2 ? 1u : 0u);
-        d.smem_bytes = nbuf * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
+        // compile-time bodies skew each lane by kLaneSkew slots
+        const uint32_t skew = d.spec ? C * kLaneSkew : 0u;
+        d.smem_bytes = nbuf * (pad_host(elems) + skew + 1u) * uint32_t(sizeof(vec2_t));
     } else {
         uint32_t t = (elems + 7) / 8;
         t = (t + 31) / 32 * 32;
