@@ -39,9 +39,6 @@ constexpr uint32_t kPassThreads = 256;
 // the first inner pass reads global memory, the last writes it, and the
 // passes between exchange through two shared-memory buffers.
 constexpr uint32_t kRegTile = 4096;
-// Slots added after every lane of a compile-time (power-of-two) tile in
-// shared memory, so that lane-major accesses spread over the banks.
-constexpr uint32_t kLaneSkew = 4;
 // Largest prime factor a DIRECT plan accepts; larger primes go to Rader/Bluestein.
 constexpr uint32_t kMaxDirectPrime = 31;
 
@@ -85,6 +82,7 @@ struct PassDesc {
     uint32_t tiles;          // ceil(batch * lanes_j / C)
     uint32_t threads;        // CTA size
     uint32_t smem_bytes;     // dynamic shared memory
+    uint32_t lane_stride;    // compile-time bodies: shared-memory slots from one lane to the next
     uint8_t load_mode, store_mode, order;
     uint8_t inv;             // butterfly direction (tables already carry it)
     uint8_t regmode;         // fused-I/O tile (radices <= 16, C*R <= kRegTile)

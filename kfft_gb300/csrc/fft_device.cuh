@@ -54,15 +54,6 @@ constexpr uint32_t kPadShift = 3;
 #endif
 __device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> kPadShift); }
 
-// Lanes of a compile-time (power-of-two) tile in shared memory: lane c starts
-// at c * lane_stride(R), its padded length plus kLaneSkew slots.  Without the
-// skew a lane is a whole number of 128-byte rows, so the lanes of a lane-major
-// access (consecutive threads on consecutive lanes, 8 lanes x 4 points per
-// warp) all fall in the same banks; with it lane c is shifted by 32c bytes and
-// such an access takes the minimum two wavefronts.
-__host__ __device__ constexpr uint32_t lane_stride(uint32_t R) {
-    return R + (R >> kPadShift) + kLaneSkew;
-}
 
 // resident CTAs per SM the fused-I/O kernels are compiled for (register cap
 // 65536 / (256 * blocks)): three for FP32, two for FP64 (more would spill)
@@ -952,7 +943,7 @@ __device__ __forceinline__ void spec_stage(const PassDesc& d, const vec2_t* __re
     constexpr bool kLinSt = (NS % kPad) == 0 || (NS == 1 && (kPad % P) == 0 && (R % kPad) == 0);
     constexpr uint32_t kLdStride = M + (M >> kPadShift);
     constexpr uint32_t kStStride = NS + (NS >> kPadShift);
-    constexpr uint32_t kLane = lane_stride(R);
+    const uint32_t lstride = d.lane_stride;
     const uint32_t items = d.C * M;
     const bool cfast = (SIO == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
                                           : ((DIO == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
@@ -986,11 +977,11 @@ __device__ __forceinline__ void spec_stage(const PassDesc& d, const vec2_t* __re
                 for (int q = 0; q < P; ++q) v[q] = {real_t(0), real_t(0)};
             }
         } else if constexpr (kLinLd) {
-            const vec2_t* p0 = src + c * kLane + pad(jj);
+            const vec2_t* p0 = src + c * lstride + pad(jj);
 #pragma unroll
             for (int q = 0; q < P; ++q) v[q] = p0[q * kLdStride];
         } else {
-            const vec2_t* l0 = src + c * kLane;
+            const vec2_t* l0 = src + c * lstride;
 #pragma unroll
             for (int q = 0; q < P; ++q) v[q] = l0[pad(jj + q * M)];
         }
@@ -1001,11 +992,11 @@ __device__ __forceinline__ void spec_stage(const PassDesc& d, const vec2_t* __re
         const uint32_t ob = blk * NS * P + kk;
         if constexpr (DIO == IO_SMEM) {
             if constexpr (kLinSt) {
-                vec2_t* p0 = dst + c * kLane + pad(ob);
+                vec2_t* p0 = dst + c * lstride + pad(ob);
 #pragma unroll
                 for (int q = 0; q < P; ++q) p0[q * kStStride] = v[q];
             } else {
-                vec2_t* l0 = dst + c * kLane;
+                vec2_t* l0 = dst + c * lstride;
 #pragma unroll
                 for (int q = 0; q < P; ++q) l0[pad(ob + q * NS)] = v[q];
             }
@@ -1060,9 +1051,9 @@ __device__ __forceinline__ void tile_loop_pipelined(const PassDesc& d, vec2_t* s
     constexpr int PL = T > 1 ? T : 16;
     constexpr uint32_t M0 = R / 16;
     const uint32_t total = d.batch * d.lanes_j;
-    constexpr uint32_t kLane = lane_stride(R);
+    const uint32_t lstride = d.lane_stride;
     vec2_t* bufA = sm;
-    vec2_t* bufB = sm + d.C * kLane + 1;
+    vec2_t* bufB = sm + d.C * lstride + 1;
     const uint32_t it = threadIdx.x;
     const bool act = it < d.C * M0;
     uint32_t c0, jj0;
@@ -1119,11 +1110,11 @@ __device__ __forceinline__ void tile_loop_pipelined(const PassDesc& d, vec2_t* s
                 if (live) fused_store<16>(d, bs, j, ob, 1, v);
             } else {
                 if constexpr (kPadShift >= 4) {
-                    vec2_t* p0 = bufA + c0 * kLane + pad(ob);  // 16 slots inside one pad period
+                    vec2_t* p0 = bufA + c0 * lstride + pad(ob);  // 16 slots inside one pad period
 #pragma unroll
                     for (int q = 0; q < 16; ++q) p0[q] = v[q];
                 } else {
-                    vec2_t* l0 = bufA + c0 * kLane;
+                    vec2_t* l0 = bufA + c0 * lstride;
 #pragma unroll
                     for (int q = 0; q < 16; ++q) l0[pad(ob + q)] = v[q];
                 }
@@ -1197,9 +1188,9 @@ __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char*
     constexpr uint32_t M0 = R / 16;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     vec2_t* raw = reinterpret_cast<vec2_t*>(smem + 128);
-    constexpr uint32_t kLane = lane_stride(R);
+    const uint32_t lstride = d.lane_stride;
     vec2_t* bufA = raw + d.C * R;
-    vec2_t* bufB = bufA + d.C * kLane + 1;
+    vec2_t* bufB = bufA + d.C * lstride + 1;
     const uint32_t total = d.batch;  // one lane per sequence (lanes_j == 1)
     const uint32_t it = threadIdx.x;
     const bool act = it < d.C * M0;
@@ -1253,7 +1244,7 @@ __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char*
             if constexpr (NP == 1) {
                 if (live) fused_store<16>(d, g, 0, ob, 1, v);
             } else {
-                vec2_t* p0 = bufA + c0 * kLane + pad(ob);  // 16 slots inside one pad period
+                vec2_t* p0 = bufA + c0 * lstride + pad(ob);  // 16 slots inside one pad period
 #pragma unroll
                 for (int q = 0; q < 16; ++q) p0[q] = v[q];
             }
@@ -1324,8 +1315,7 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
     vec2_t* bufB = sm + pad(d.C * d.R) + 1;
 #if defined(KFFT_HALF_SCALAR)
     if constexpr (SPEC) {
-        // compile-time bodies lay lanes out at lane_stride(R)
-        if (d.spec) bufB = sm + d.C * lane_stride(d.R) + 1;
+        if (d.spec) bufB = sm + d.C * d.lane_stride + 1;
     }
     if constexpr (SPEC) switch (d.spec) {
         case 4: tile_body_spec<16, INV>(d, lane0, total, bufA, bufB); return;

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_pass_spec(
     const __grid_constant__ PassDesc d) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     vec2_t* sm = reinterpret_cast<vec2_t*>(smem_raw);
-    tile_body_spec<R, INV>(d, blockIdx.x * d.C, d.batch * d.lanes_j, sm, sm + d.C * lane_stride(R) + 1);
+    tile_body_spec<R, INV>(d, blockIdx.x * d.C, d.batch * d.lanes_j, sm, sm + d.C * d.lane_stride + 1);
 }
 
 // Set when a bulk-copy wait of k_pass_bulk ran out (only a failed copy can

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <sstream>
 
 #include "engine.cuh"
@@ -46,6 +47,109 @@ static uint32_t tile_capacity() {
 
 static uint32_t smem_for(uint32_t elems) {
     return 2u * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory lane stride of the compile-time (power-of-two) tile bodies
+// ---------------------------------------------------------------------------
+static std::vector<uint8_t> inner_radices(uint32_t R);
+
+// Shared-memory wavefronts of one warp-wide access to 8-byte elements at the
+// slots `idx` (-1: thread idle): each half-warp is one request of up to 128
+// bytes, which takes as many wavefronts as the most distinct elements that
+// share a bank pair (slot mod 16).
+static uint32_t smem_wavefronts(const int64_t* idx) {
+    uint32_t total = 0;
+    for (int h = 0; h < 2; ++h) {
+        int64_t seen[16];
+        int n = 0;
+        uint32_t per[16] = {0};
+        for (int t = 16 * h; t < 16 * h + 16; ++t) {
+            if (idx[t] < 0) continue;
+            bool dup = false;
+            for (int i = 0; i < n; ++i) dup = dup || seen[i] == idx[t];
+            if (dup) continue;
+            seen[n++] = idx[t];
+            ++per[idx[t] % 16];
+        }
+        uint32_t worst = 0;
+        for (uint32_t v : per) worst = std::max(worst, v);
+        total += worst;
+    }
+    return total;
+}
+
+// Wavefronts of the shared-memory accesses of one tile iteration of the
+// compile-time body for a pass length R (radices 16, ..., 16, T) with C lanes
+// at `stride` slots apart.  Lane-major stages (a global access in lane mode)
+// put consecutive threads on consecutive lanes; the others on consecutive
+// butterflies of one lane.
+static uint64_t spec_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool load_lane,
+                               bool store_lane) {
+    auto padh = [](uint64_t i) { return i + (i >> 4); };
+    const std::vector<uint8_t> rad = inner_radices(R);
+    const size_t np = rad.size();
+    uint64_t cost = 0;
+    uint32_t NS = 1;
+    int64_t idx[32];
+    for (size_t st = 0; st < np; ++st) {
+        const uint32_t P = rad[st], M = R / P, items = C * M;
+        const bool last = st + 1 == np;
+        const bool cfast = (st == 0 && load_lane) || (last && store_lane);
+        const uint32_t warps = std::min<uint32_t>(kPassThreads / 32, (items + 31) / 32);
+        for (uint32_t w = 0; w < warps; ++w) {
+            for (uint32_t q = 0; q < P; ++q) {
+                for (int rw = 0; rw < 2; ++rw) {
+                    if ((rw == 0 && st == 0) || (rw == 1 && last)) continue;
+                    for (uint32_t t = 0; t < 32; ++t) {
+                        const uint32_t it = w * 32 + t;
+                        if (it >= items) {
+                            idx[t] = -1;
+                            continue;
+                        }
+                        uint32_t c, jj;
+                        if (cfast) {
+                            jj = it / C;
+                            c = it % C;
+                        } else {
+                            c = it / M;
+                            jj = it % M;
+                        }
+                        const uint64_t ob = uint64_t(jj / NS) * NS * P + jj % NS;
+                        const uint64_t slot = rw == 0 ? padh(jj + uint64_t(q) * M) : padh(ob + uint64_t(q) * NS);
+                        idx[t] = int64_t(uint64_t(c) * stride + slot);
+                    }
+                    cost += smem_wavefronts(idx);
+                }
+            }
+        }
+        NS *= P;
+    }
+    return cost;
+}
+
+// The padded lane length plus the skew (0..15 slots) with the fewest
+// shared-memory wavefronts per tile: without a skew the lanes of a lane-major
+// access can all fall in the same banks.  FP32 only (8-byte elements).
+static uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane) {
+    static std::mutex mu;
+    static std::map<std::pair<uint64_t, uint32_t>, uint32_t> cache;
+    const auto key = std::make_pair((uint64_t(R) << 32) | C, uint32_t(load_lane) | (uint32_t(store_lane) << 1));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const uint32_t base = R + (R >> 4);
+    uint32_t best = base;
+    uint64_t best_cost = ~uint64_t(0);
+    for (uint32_t skew = 0; skew < 16; ++skew) {
+        const uint64_t c = spec_smem_cost(R, C, base + skew, load_lane, store_lane);
+        if (c < best_cost) {
+            best_cost = c;
+            best = base + skew;
+        }
+    }
+    cache[key] = best;
+    return best;
 }
 
 // ---------------------------------------------------------------------------
@@ -544,7 +648,14 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     const uint32_t cap = tile_capacity();
     uint32_t C;
     if (d.order == ORDER_B) {
-        C = std::min<uint32_t>(16, std::max<uint32_t>(1, cap / s.R));
+        // consecutive lanes are consecutive sequences (columns of a 2D
+        // array): at least 16 (128-byte segments), and, as for row lanes
+        // below, enough that every thread has a butterfly in every inner stage
+        uint32_t want = 16;
+        const uint32_t share = s.R >= 256 ? 2u : 1u;
+        for (uint8_t r : s.radices)
+            want = std::max<uint32_t>(want, (kPassThreads * r + share * s.R - 1) / (share * s.R));
+        C = std::min<uint32_t>(want, std::max<uint32_t>(1, cap / s.R));
         C = std::min(C, d.batch);
         d.load_mode = MODE_LANE;
         d.store_mode = MODE_LANE;
@@ -605,9 +716,13 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     if (d.regmode) {
         d.threads = kPassThreads;
         const uint32_t nbuf = s.radices.size() >= 3 ? 2u : (s.radices.size() == 2 ? 1u : 0u);
-        // compile-time bodies skew each lane by kLaneSkew slots
-        const uint32_t skew = d.spec ? C * kLaneSkew : 0u;
-        d.smem_bytes = nbuf * (pad_host(elems) + skew + 1u) * uint32_t(sizeof(vec2_t));
+        if (d.spec) {
+            d.lane_stride = spec_lane_stride(s.R, C, d.load_mode == MODE_LANE,
+                                             d.store_mode == MODE_LANE);
+            d.smem_bytes = nbuf * (C * d.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
+        } else {
+            d.smem_bytes = nbuf * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
+        }
     } else {
         uint32_t t = (elems + 7) / 8;
         t = (t + 31) / 32 * 32;
