@@ -176,8 +176,11 @@ struct PassSpec {
 struct DeviceArena;  // device memory owned by a plan tree
 
 // Planner knobs one plan variant fixes (the tuner's search space).
+#ifndef KFFT_PLAN_RMAX
+#define KFFT_PLAN_RMAX 1024
+#endif
 struct PlanVariant {
-    uint32_t rmax = 1024;        // largest pass length of a multi-pass split
+    uint32_t rmax = KFFT_PLAN_RMAX;  // largest pass length of a multi-pass split
     uint32_t lanes = 0;          // lanes of multi-pass tiles (0: precision default)
     uint32_t single_cap = 4096;  // longest length run as one fused pass
     bool no_fused = false;       // shared-memory ping-pong tiles only

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -36,6 +37,19 @@ constexpr uint32_t kPadShiftHost = 3;
 constexpr uint32_t kMultiLanes = 4;   // 64-byte row segments
 #endif
 constexpr uint32_t kMultiRmax = 1024;
+
+// Multi-lane tiles of passes of 256 points or more hold half a full tile in
+// the FP64 build (measured faster there); FP32 tiles are full (with lanes
+// skewed in shared memory, a full tile of a 256-point pass measured 18-23%
+// faster than half of one).
+static uint32_t lane_share(uint32_t R) {
+#if defined(KFFT_HALF_SCALAR)
+    (void)R;
+    return 1;
+#else
+    return R >= 256 ? 2u : 1u;
+#endif
+}
 
 static uint32_t pad_host(uint32_t i) { return i + (i >> kPadShiftHost); }
 
@@ -370,14 +384,32 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1)) {
         Rs.push_back(N);
     } else if (small_radices) {
+#if defined(KFFT_HALF_SCALAR)
+        const bool pow2 = (N & (N - 1)) == 0;
+#else
+        const bool pow2 = false;
+#endif
+        double best = -1.0;
         for (uint32_t rmax : {1024u, 768u, 512u, 384u, 256u, 128u, 64u, 32u, 16u}) {
             if (rmax > V.rmax) continue;
             std::vector<uint32_t> cand = split_passes(N, rmax);
             bool ok = !cand.empty();
             for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R));
-            if (ok) {
+            if (!ok) continue;
+            if (!pow2) {
                 Rs = cand;
                 break;
+            }
+            // FP32 powers of two (compile-time bodies): the split with the
+            // least estimated time, a pass of up to 256 points counting 1 and
+            // each doubling beyond it 0.5 more (its tiles hold fewer lanes,
+            // so its row segments are narrower: 64 bytes at 512 points, 32 at
+            // 1024); ties go to fewer passes
+            double cost = 0.0;
+            for (uint32_t R : cand) cost += R <= 256 ? 1.0 : 1.0 + 0.5 * std::log2(R / 256.0);
+            if (best < 0.0 || cost < best - 1e-9) {
+                best = cost;
+                Rs = cand;
             }
         }
     }
@@ -652,7 +684,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         // array): at least 16 (128-byte segments), and, as for row lanes
         // below, enough that every thread has a butterfly in every inner stage
         uint32_t want = 16;
-        const uint32_t share = s.R >= 256 ? 2u : 1u;
+        const uint32_t share = lane_share(s.R);
         for (uint8_t r : s.radices)
             want = std::max<uint32_t>(want, (kPassThreads * r + share * s.R - 1) / (share * s.R));
         C = std::min<uint32_t>(want, std::max<uint32_t>(1, cap / s.R));
@@ -666,12 +698,11 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.load_mode = MODE_ELEM;
         d.store_mode = MODE_ELEM;
     } else {
-        // enough lanes that every thread has a butterfly in every inner stage
-        // (C * R / radix >= threads) for passes up to 128 points, half the
-        // threads from 256 points up (measured faster there than a full
-        // tile), and at least kMultiLanes for row segments
+        // enough lanes that every thread (or half of them, lane_share) has a
+        // butterfly in every inner stage (C * R / radix >= threads), and at
+        // least kMultiLanes for row segments
         uint32_t want = kMultiLanes;
-        const uint32_t share = s.R >= 256 ? 2u : 1u;
+        const uint32_t share = lane_share(s.R);
         for (uint8_t r : s.radices)
             want = std::max<uint32_t>(want, (kPassThreads * r + share * s.R - 1) / (share * s.R));
         C = std::min(P.var.lanes ? P.var.lanes : want, d.lanes_j);
