@@ -252,6 +252,11 @@ bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t*
                   const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
 // Descriptor of pass `pass` of a DIRECT plan (no fused element operations).
+// Shared-memory slots from one lane to the next in a compile-time
+// (power-of-two) tile body of C lanes of R points run by `threads` threads:
+// the padded lane plus the skew with the fewest bank conflicts.
+uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
+                          uint32_t threads);
 PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const Layout& lin,
                         vec2_t* out, const Layout& lout, real_t scale);
 

@@ -705,7 +705,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
             }
         } else {
 #pragma unroll
-            for (int q = 0; q < P; ++q) v[q] = src[pad(c * d.R + jj + q * m)];
+            for (int q = 0; q < P; ++q) v[q] = src[c * d.lane_stride + pad(jj + q * m)];
         }
         const uint32_t blk = fdiv(jj, st.div_ns);
         const uint32_t kk = jj - blk * st.ns;
@@ -714,7 +714,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         const uint32_t ob = blk * st.ns * P + kk;
         if (dio == IO_SMEM) {
 #pragma unroll
-            for (int q = 0; q < P; ++q) dst[pad(c * d.R + ob + q * st.ns)] = v[q];
+            for (int q = 0; q < P; ++q) dst[c * d.lane_stride + pad(ob + q * st.ns)] = v[q];
         } else if (live) {
             fused_store<P>(d, bs, j, ob, st.ns, v);
         }
@@ -846,7 +846,7 @@ __device__ __forceinline__ void tc_pass16(const PassDesc& d, const InnerStep& st
                 }
             } else {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) x[u] = src[pad(c * d.R + jj + uint32_t(ks[u]) * m)];
+                for (int u = 0; u < 4; ++u) x[u] = src[c * d.lane_stride + pad(jj + uint32_t(ks[u]) * m)];
             }
             if (st.ns > 1) {
                 const uint32_t blk = fdiv(jj, st.div_ns);
@@ -898,8 +898,8 @@ __device__ __forceinline__ void tc_pass16(const PassDesc& d, const InnerStep& st
             const vec2_t o0 = {yr[e] * un, yi[e] * un};          // output gq
             const vec2_t o1 = {yr[2 + e] * un, yi[2 + e] * un};  // output gq + 8
             if (dio == IO_SMEM) {
-                dst[pad(co * d.R + ob + uint32_t(gq) * st.ns)] = o0;
-                dst[pad(co * d.R + ob + uint32_t(gq + 8) * st.ns)] = o1;
+                dst[co * d.lane_stride + pad(ob + uint32_t(gq) * st.ns)] = o0;
+                dst[co * d.lane_stride + pad(ob + uint32_t(gq + 8) * st.ns)] = o1;
             } else {
                 const uint32_t g = lane0 + co;
                 if (g >= total) continue;
@@ -1283,8 +1283,8 @@ __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const I
 
 // A tile whose first inner pass reads global memory and whose last writes it:
 // two shared-memory round trips fewer than tile_body.  Shared memory holds two
-// buffers of pad(C*R)+1 elements (only when the sub-FFT has 3+ inner passes;
-// one buffer for 2 passes; none for 1).
+// buffers of C*lane_stride+1 elements, lane c at c*lane_stride (only when the
+// sub-FFT has 3+ inner passes; one buffer for 2 passes; none for 1).
 // SPEC: dispatch power-of-two passes (d.spec) to their compile-time bodies;
 // the pass kernel launches those as kernels of their own and leaves it off.
 // TC: keep the tensor-core radix-16 stage; the queue kernel leaves it off
@@ -1312,11 +1312,8 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
         return;
     }
     vec2_t* bufA = sm;
-    vec2_t* bufB = sm + pad(d.C * d.R) + 1;
+    vec2_t* bufB = sm + d.C * d.lane_stride + 1;
 #if defined(KFFT_HALF_SCALAR)
-    if constexpr (SPEC) {
-        if (d.spec) bufB = sm + d.C * d.lane_stride + 1;
-    }
     if constexpr (SPEC) switch (d.spec) {
         case 4: tile_body_spec<16, INV>(d, lane0, total, bufA, bufB); return;
         case 5: tile_body_spec<32, INV>(d, lane0, total, bufA, bufB); return;

@@ -31,6 +31,17 @@ __global__ void __launch_bounds__(kPassThreads, 2) k_pass_pipe(const __grid_cons
     tile_loop_pipelined<R, INV>(d, reinterpret_cast<vec2_t*>(smem_raw));
 }
 
+// k_pass_pipe with twice the threads and twice the lanes per tile (8192
+// points): multi-lane passes of 512 or 1024 points, whose 4096-point tiles
+// hold only 8 or 4 lanes (64- or 32-byte row segments), read and write twice
+// as wide segments.  One CTA per SM.  (256-point passes, whose 4096-point
+// tiles already hold 16 lanes, measured slower on it.)
+template <uint32_t R, bool INV>
+__global__ void __launch_bounds__(2 * kPassThreads, 1) k_pass_pipe_wide(const __grid_constant__ PassDesc d) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_loop_pipelined<R, INV>(d, reinterpret_cast<vec2_t*>(smem_raw));
+}
+
 template <uint32_t R, bool INV>
 __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_pass_spec(
     const __grid_constant__ PassDesc d) {
@@ -53,10 +64,20 @@ __global__ void __launch_bounds__(kPassThreads, 2) k_pass_bulk(const __grid_cons
 
 using SpecKernel = void (*)(PassDesc);
 
-enum SpecKind { SPEC_ONE_TILE = 0, SPEC_PIPE = 1, SPEC_BULK = 2 };
+// shortest pass that runs on the wide tiles
+#ifndef KFFT_WIDE_MIN_R
+#define KFFT_WIDE_MIN_R 512
+#endif
+
+enum SpecKind { SPEC_ONE_TILE = 0, SPEC_PIPE = 1, SPEC_BULK = 2, SPEC_WIDE = 3 };
 
 template <uint32_t R>
 SpecKernel pick(int kind, bool inv) {
+    if constexpr (R >= 256 && R <= 1024) {
+        if (kind == SPEC_WIDE) return inv ? k_pass_pipe_wide<R, true> : k_pass_pipe_wide<R, false>;
+    } else {
+        if (kind == SPEC_WIDE) return nullptr;
+    }
     if (kind == SPEC_BULK) return inv ? k_pass_bulk<R, true> : k_pass_bulk<R, false>;
     if (kind == SPEC_PIPE) return inv ? k_pass_pipe<R, true> : k_pass_pipe<R, false>;
     return inv ? k_pass_spec<R, true> : k_pass_spec<R, false>;
@@ -82,7 +103,7 @@ namespace {
 #if defined(KFFT_HALF_SCALAR)
 // Raises the dynamic shared-memory limit of a kernel once and caches its
 // resident CTAs per SM for a shared-memory size.
-int prepare(SpecKernel f, uint32_t smem) {
+int prepare(SpecKernel f, uint32_t smem, uint32_t threads = kPassThreads) {
     static std::mutex mu;
     static std::map<std::pair<SpecKernel, uint32_t>, int> cache;
     static std::map<SpecKernel, bool> configured;
@@ -99,7 +120,7 @@ int prepare(SpecKernel f, uint32_t smem) {
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)f, kPassThreads, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)f, int(threads), smem) !=
         cudaSuccess) {
         cudaGetLastError();
         n = 0;
@@ -148,6 +169,29 @@ void launch_pass_reg(const PassDesc& d, const PassExtra& x, cudaStream_t st) {
             const uint32_t grid = uint32_t(std::max(per_sm, 0)) * uint32_t(sm_count());
             if (per_sm > 0 && d.tiles >= 2 * grid) {
                 f<<<grid, kPassThreads, smem, st>>>(d);
+                note_cuda_error(cudaGetLastError());
+                count_launch();
+                return;
+            }
+        }
+        // multi-lane rows of 256-1024 points with a full 4096-point tile:
+        // the same pass on 8192-point tiles of twice the lanes
+        if (d.pro_op == PRO_NONE && d.order == ORDER_J && d.R >= KFFT_WIDE_MIN_R && d.R <= 1024 &&
+            d.C * d.R == kRegTile && d.lanes_j >= 2 * d.C) {
+            SpecKernel f = spec_kernel(d.spec, SPEC_WIDE, inv);
+            PassDesc w = d;
+            w.C = 2 * d.C;
+            w.div_C.init(w.C);
+            w.tiles = uint32_t((uint64_t(d.batch) * d.lanes_j + w.C - 1) / w.C);
+            w.threads = 2 * kPassThreads;
+            w.lane_stride = spec_lane_stride(d.R, w.C, d.load_mode == MODE_LANE,
+                                             d.store_mode == MODE_LANE, w.threads);
+            const uint32_t nbuf = d.R == 256 ? 1u : 2u;  // stages 16,16 or 16,16,T
+            w.smem_bytes = nbuf * (w.C * w.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
+            const int per_sm = f ? prepare(f, w.smem_bytes, w.threads) : -1;
+            const uint32_t grid = uint32_t(std::max(per_sm, 0)) * uint32_t(sm_count());
+            if (per_sm > 0 && w.tiles >= 2 * grid) {
+                f<<<grid, w.threads, w.smem_bytes, st>>>(w);
                 note_cuda_error(cudaGetLastError());
                 count_launch();
                 return;

@@ -64,27 +64,30 @@ static uint32_t smem_for(uint32_t elems) {
 }
 
 // ---------------------------------------------------------------------------
-// shared-memory lane stride of the compile-time (power-of-two) tile bodies
+// shared-memory lane stride of the register-tile bodies
 // ---------------------------------------------------------------------------
 static std::vector<uint8_t> inner_radices(uint32_t R);
 
-// Shared-memory wavefronts of one warp-wide access to 8-byte elements at the
-// slots `idx` (-1: thread idle): each half-warp is one request of up to 128
-// bytes, which takes as many wavefronts as the most distinct elements that
-// share a bank pair (slot mod 16).
+// Elements per 128-byte shared-memory row (one request of a warp-wide access).
+constexpr uint32_t kRowElems = 128 / sizeof(vec2_t);
+
+// Shared-memory wavefronts of one warp-wide access to the element slots `idx`
+// (-1: thread idle): every kRowElems threads form one request, which takes as
+// many wavefronts as the most distinct elements that share a bank group
+// (slot mod kRowElems).
 static uint32_t smem_wavefronts(const int64_t* idx) {
     uint32_t total = 0;
-    for (int h = 0; h < 2; ++h) {
-        int64_t seen[16];
-        int n = 0;
-        uint32_t per[16] = {0};
-        for (int t = 16 * h; t < 16 * h + 16; ++t) {
+    for (uint32_t h = 0; h < 32; h += kRowElems) {
+        int64_t seen[kRowElems];
+        uint32_t n = 0;
+        uint32_t per[kRowElems] = {0};
+        for (uint32_t t = h; t < h + kRowElems; ++t) {
             if (idx[t] < 0) continue;
             bool dup = false;
-            for (int i = 0; i < n; ++i) dup = dup || seen[i] == idx[t];
+            for (uint32_t i = 0; i < n; ++i) dup = dup || seen[i] == idx[t];
             if (dup) continue;
             seen[n++] = idx[t];
-            ++per[idx[t] % 16];
+            ++per[idx[t] % kRowElems];
         }
         uint32_t worst = 0;
         for (uint32_t v : per) worst = std::max(worst, v);
@@ -93,14 +96,14 @@ static uint32_t smem_wavefronts(const int64_t* idx) {
     return total;
 }
 
-// Wavefronts of the shared-memory accesses of one tile iteration of the
-// compile-time body for a pass length R (radices 16, ..., 16, T) with C lanes
-// at `stride` slots apart.  Lane-major stages (a global access in lane mode)
-// put consecutive threads on consecutive lanes; the others on consecutive
-// butterflies of one lane.
-static uint64_t spec_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool load_lane,
-                               bool store_lane) {
-    auto padh = [](uint64_t i) { return i + (i >> 4); };
+// Wavefronts of the shared-memory accesses of one tile iteration of a
+// register-tile body (inner radices of R, C lanes `stride` slots apart, run
+// by `threads` threads).  Stages with a global access in lane mode put
+// consecutive threads on consecutive lanes; the others put them on
+// consecutive butterflies of one lane.
+static uint64_t tile_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool load_lane,
+                               bool store_lane, uint32_t threads) {
+    auto padh = [](uint64_t i) { return i + i / kRowElems; };
     const std::vector<uint8_t> rad = inner_radices(R);
     const size_t np = rad.size();
     uint64_t cost = 0;
@@ -110,7 +113,7 @@ static uint64_t spec_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool loa
         const uint32_t P = rad[st], M = R / P, items = C * M;
         const bool last = st + 1 == np;
         const bool cfast = (st == 0 && load_lane) || (last && store_lane);
-        const uint32_t warps = std::min<uint32_t>(kPassThreads / 32, (items + 31) / 32);
+        const uint32_t warps = std::min<uint32_t>(threads / 32, (items + 31) / 32);
         for (uint32_t w = 0; w < warps; ++w) {
             for (uint32_t q = 0; q < P; ++q) {
                 for (int rw = 0; rw < 2; ++rw) {
@@ -142,24 +145,29 @@ static uint64_t spec_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool loa
     return cost;
 }
 
-// The padded lane length plus the skew (0..15 slots) with the fewest
-// shared-memory wavefronts per tile: without a skew the lanes of a lane-major
-// access can all fall in the same banks.  FP32 only (8-byte elements).
-static uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane) {
+// The padded lane length plus the skew (0 .. kRowElems-1 slots) with the
+// fewest shared-memory wavefronts per tile: without a skew the lanes of a
+// lane-major access can all fall in the same banks (a lane of 2^k >= 16
+// points is a whole number of 128-byte rows).  Ties go to the smaller skew.
+uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
+                          uint32_t threads) {
     static std::mutex mu;
     static std::map<std::pair<uint64_t, uint32_t>, uint32_t> cache;
-    const auto key = std::make_pair((uint64_t(R) << 32) | C, uint32_t(load_lane) | (uint32_t(store_lane) << 1));
+    const auto key = std::make_pair((uint64_t(R) << 32) | C,
+                                    uint32_t(load_lane) | (uint32_t(store_lane) << 1) | (threads << 2));
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    const uint32_t base = R + (R >> 4);
+    const uint32_t base = R + R / kRowElems;
     uint32_t best = base;
     uint64_t best_cost = ~uint64_t(0);
-    for (uint32_t skew = 0; skew < 16; ++skew) {
-        const uint64_t c = spec_smem_cost(R, C, base + skew, load_lane, store_lane);
-        if (c < best_cost) {
-            best_cost = c;
-            best = base + skew;
+    if (C > 1 && inner_radices(R).size() > 1) {
+        for (uint32_t skew = 0; skew < kRowElems; ++skew) {
+            const uint64_t c = tile_smem_cost(R, C, base + skew, load_lane, store_lane, threads);
+            if (c < best_cost) {
+                best_cost = c;
+                best = base + skew;
+            }
         }
     }
     cache[key] = best;
@@ -747,13 +755,9 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
     if (d.regmode) {
         d.threads = kPassThreads;
         const uint32_t nbuf = s.radices.size() >= 3 ? 2u : (s.radices.size() == 2 ? 1u : 0u);
-        if (d.spec) {
-            d.lane_stride = spec_lane_stride(s.R, C, d.load_mode == MODE_LANE,
-                                             d.store_mode == MODE_LANE);
-            d.smem_bytes = nbuf * (C * d.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
-        } else {
-            d.smem_bytes = nbuf * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
-        }
+        d.lane_stride = spec_lane_stride(s.R, C, d.load_mode == MODE_LANE,
+                                         d.store_mode == MODE_LANE, kPassThreads);
+        d.smem_bytes = nbuf * (C * d.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
     } else {
         uint32_t t = (elems + 7) / 8;
         t = (t + 31) / 32 * 32;
