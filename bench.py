@@ -854,11 +854,13 @@ def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, devi
 
 
 # DRAM bytes per launch of the dominant kernel from ncu captures
-# (dram__bytes_read.sum + dram__bytes_write.sum).  The uneven batch is too
-# large for a full-set capture: every 8th sequence was captured (37.47 M
-# points, 2.099 GB) and scaled by points, which the same length mix allows.
-NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.087e9 / 37465227}
-NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.3e6, "c2c_f32_2p18x64": 219.5e6}
+# (dram__bytes_read.sum + dram__bytes_write.sum, averaged over the captured
+# pass launches).  The uneven batch is too large for a full-set capture:
+# every 8th sequence was captured (37.47 M points, 2.263 GB) and scaled by
+# points, which the same length mix allows.
+NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.263e9 / 37465227}
+NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.3e6, "c2c_f32_2p18x64": 217.7e6,
+                             "c2c_f32_2p20x16": 215.7e6, "c2c_f32_2p24": 215.9e6}
 
 
 def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_step=None,
@@ -884,7 +886,7 @@ def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_ste
         traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(workload)
         return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "k_pass_reg / k_pass_pipe (one launch per pass)",
+                "kernel": "k_pass_bulk / k_pass_pipe / k_pass_pipe_wide (one launch per pass)",
                 "launches_per_step": n, "launch_ms": round(dur, 4),
                 "per_transform_gbs": round(per_transform, 1)}
     # the uneven batch: one k_persistent launch runs every pass of every sequence
