@@ -576,9 +576,12 @@ KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* 
         for (uint32_t k = 0; k < chunks; ++k) {
             const uint32_t b0 = uint32_t(uint64_t(batch) * k / chunks);
             const uint32_t b1 = uint32_t(uint64_t(batch) * (k + 1) / chunks);
-            const size_t off = size_t(b0) * P.N, cb = per * (b1 - b0);
+            const size_t off = size_t(b0) * P.N;
+            const CopyRange cr = copy_range(per * b0, per * b1, bytes, k == 0, k + 1 == chunks);
             if (hin) {
-                cudaMemcpyAsync(stage_in + off, fin + off, cb, cudaMemcpyHostToDevice, cs->in);
+                cudaMemcpyAsync(reinterpret_cast<char*>(stage_in) + cr.in0,
+                                reinterpret_cast<const char*>(fin) + cr.in0, cr.in1 - cr.in0,
+                                cudaMemcpyHostToDevice, cs->in);
                 cudaEvent_t e = evs.get();
                 if (!e) return KFFT_RET_BUFFER_FAIL;
                 cudaEventRecord(e, cs->in);
@@ -591,7 +594,9 @@ KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* 
                 if (!e) return KFFT_RET_BUFFER_FAIL;
                 cudaEventRecord(e, st);
                 cudaStreamWaitEvent(cs->out, e, 0);
-                cudaMemcpyAsync(fout + off, dout + off, cb, cudaMemcpyDeviceToHost, cs->out);
+                cudaMemcpyAsync(reinterpret_cast<char*>(fout) + cr.out0,
+                                reinterpret_cast<const char*>(dout) + cr.out0, cr.out1 - cr.out0,
+                                cudaMemcpyDeviceToHost, cs->out);
             }
         }
         if (hout) {

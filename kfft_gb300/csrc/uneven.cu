@@ -241,10 +241,16 @@ kfft_return_t launch(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2
 
 // Contiguous groups of about equal points for the host-buffer path: copies
 // of one group overlap the transform of its neighbours.
+#ifndef KFFT_UNEVEN_GROUPS
+#define KFFT_UNEVEN_GROUPS 16
+#endif
+#ifndef KFFT_UNEVEN_GROUP_LOG2
+#define KFFT_UNEVEN_GROUP_LOG2 23
+#endif
 void make_groups(kfft_plan_uneven* P) {
-    constexpr uint64_t kGroupPoints = uint64_t(1) << 23;
+    constexpr uint64_t kGroupPoints = uint64_t(1) << KFFT_UNEVEN_GROUP_LOG2;
     const size_t count = P->lengths.size();
-    const uint64_t k = std::min<uint64_t>(16, P->total / kGroupPoints);
+    const uint64_t k = std::min<uint64_t>(KFFT_UNEVEN_GROUPS, P->total / kGroupPoints);
     if (k < 2 || count < 2) return;
     std::vector<std::pair<size_t, size_t>> ranges;
     size_t s = 0;
@@ -366,10 +372,14 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_c
             return e;
         };
         kfft_return_t r = KFFT_RET_SUCCESS;
-        for (UnevenQueue& Q : plan->groups) {
-            const size_t gb = sizeof(vec2_t) * (Q.p1 - Q.p0);
+        for (size_t g = 0; g < plan->groups.size(); ++g) {
+            UnevenQueue& Q = plan->groups[g];
+            const CopyRange cr = copy_range(sizeof(vec2_t) * Q.p0, sizeof(vec2_t) * Q.p1, bytes,
+                                            g == 0, g + 1 == plan->groups.size());
             if (hin) {
-                cudaMemcpyAsync(s_in + Q.p0, fin + Q.p0, gb, cudaMemcpyHostToDevice, cp->in);
+                cudaMemcpyAsync(reinterpret_cast<char*>(s_in) + cr.in0,
+                                reinterpret_cast<const char*>(fin) + cr.in0, cr.in1 - cr.in0,
+                                cudaMemcpyHostToDevice, cp->in);
                 cudaEvent_t e = event();
                 if (!e) {
                     r = KFFT_RET_BUFFER_FAIL;
@@ -389,7 +399,9 @@ KFFT_API kfft_return_t kfft_eval_cpx_uneven(kfft_plan_uneven* plan, const kfft_c
                 }
                 cudaEventRecord(e, st);
                 cudaStreamWaitEvent(cp->out, e, 0);
-                cudaMemcpyAsync(fout + Q.p0, s_out + Q.p0, gb, cudaMemcpyDeviceToHost, cp->out);
+                cudaMemcpyAsync(reinterpret_cast<char*>(fout) + cr.out0,
+                                reinterpret_cast<const char*>(dout) + cr.out0, cr.out1 - cr.out0,
+                                cudaMemcpyDeviceToHost, cp->out);
             }
         }
         if (hout) {

@@ -26,8 +26,9 @@ def _device_result_batch(lib, plan, x, batch):
 
 
 @pytest.mark.parametrize("inplace", [False, True])
-def test_chunked_host_batch_matches_device_path(libf, inplace):
-    n, batch = 1 << 16, 160            # 80 MiB each way: split into chunks
+@pytest.mark.parametrize("n,batch", [(1 << 16, 160),   # 80 MiB each way: split into chunks
+                                     (3000, 3000)])    # 72 MB; chunk ends off 256-byte boundaries
+def test_chunked_host_batch_matches_device_path(libf, inplace, n, batch):
     rng = np.random.default_rng(21)
     x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
     p = libf._plan("kfft_config_cpx", n, 0)
@@ -40,7 +41,7 @@ def test_chunked_host_batch_matches_device_path(libf, inplace):
             y = np.empty_like(x)
             assert libf.L.kfft_eval_cpx_batch(p, x.ctypes.data, y.ctypes.data, batch) == 0
         assert np.array_equal(y, ref)
-        for b in (0, 77, batch - 1):
+        for b in (0, 77, batch // 2, batch - 1):
             assert rel_l2(y[b], O.fft_cpx(x[b])) <= TOL32
     finally:
         libf.cleanup(p)
