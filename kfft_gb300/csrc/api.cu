@@ -309,6 +309,60 @@ struct EventSet {
     }
 };
 
+// A batched call whose input and/or output is in host memory, split into
+// `chunks` ranges of sequences: chunk k's copy in, transform (`run(b0, b1)`
+// on the compute stream `st`) and copy out run on three streams, so the
+// copies of one chunk overlap the transforms of its neighbours.  in_per and
+// out_per are bytes per sequence; h_in/h_out are the host buffers (null when
+// that side is on the device) and d_in/d_out their device counterparts.
+// The host buffers must not overlap.
+template <class Run>
+kfft_return_t chunked_host_call(uint32_t batch, uint32_t chunks, size_t in_per, size_t out_per,
+                                const void* h_in, void* d_in, void* h_out, const void* d_out,
+                                cudaStream_t st, Run run) {
+    CopyStreams* cs = copy_streams();
+    if (!cs) return KFFT_RET_BUFFER_FAIL;
+    EventSet evs;
+    const size_t tin = in_per * batch, tout = out_per * batch;
+    for (uint32_t k = 0; k < chunks; ++k) {
+        const uint32_t b0 = uint32_t(uint64_t(batch) * k / chunks);
+        const uint32_t b1 = uint32_t(uint64_t(batch) * (k + 1) / chunks);
+        const bool first = k == 0, last = k + 1 == chunks;
+        if (h_in) {
+            const CopyRange cr = copy_range(in_per * b0, in_per * b1, tin, first, last);
+            cudaMemcpyAsync(static_cast<char*>(d_in) + cr.in0, static_cast<const char*>(h_in) + cr.in0,
+                            cr.in1 - cr.in0, cudaMemcpyHostToDevice, cs->in);
+            cudaEvent_t e = evs.get();
+            if (!e) return KFFT_RET_BUFFER_FAIL;
+            cudaEventRecord(e, cs->in);
+            cudaStreamWaitEvent(st, e, 0);
+        }
+        if (!run(b0, b1)) return KFFT_RET_BUFFER_FAIL;
+        if (h_out) {
+            const CopyRange cr = copy_range(out_per * b0, out_per * b1, tout, first, last);
+            cudaEvent_t e = evs.get();
+            if (!e) return KFFT_RET_BUFFER_FAIL;
+            cudaEventRecord(e, st);
+            cudaStreamWaitEvent(cs->out, e, 0);
+            cudaMemcpyAsync(static_cast<char*>(h_out) + cr.out0,
+                            static_cast<const char*>(d_out) + cr.out0, cr.out1 - cr.out0,
+                            cudaMemcpyDeviceToHost, cs->out);
+        }
+    }
+    if (h_out) {
+        cudaEvent_t e = evs.get();
+        if (!e) return KFFT_RET_BUFFER_FAIL;
+        cudaEventRecord(e, cs->out);
+        cudaStreamWaitEvent(st, e, 0);
+    }
+    return finish(st);
+}
+
+bool ranges_overlap(const void* a, size_t na, const void* b, size_t nb) {
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + nb && y < x + na;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -791,14 +845,30 @@ KFFT_API kfft_return_t kfft_eval_scalar_batch(kfft_plan_sclr* plan, const kfft_s
     if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;  // nothing to carve: no buffer needed
     const real_t* din = reinterpret_cast<const real_t*>(fin);
     vec2_t* dout = reinterpret_cast<vec2_t*>(fout);
+    const int expand = (plan->flags & KFFT_FLAG_EXPAND_SCALAR) ? 1 : 0;
+    const uint32_t chunks = ((hin || hout) && !(hin && hout && ranges_overlap(fin, ib, fout, ob)))
+                                ? host_chunks(std::max(ib, ob), batch) : 1;
+    if (chunks > 1) {
+        // staging for the host sides, then scratch for the largest chunk
+        if (hin) din = static_cast<const real_t*>(cv.take(ib));
+        if (hout) dout = static_cast<vec2_t*>(cv.take(ob));
+        Carve scratch = cv;
+        const size_t n = plan->nfft;
+        return chunked_host_call(batch, chunks, sizeof(real_t) * n, sizeof(vec2_t) * bins,
+                                 hin ? fin : nullptr, const_cast<real_t*>(din),
+                                 hout ? fout : nullptr, dout, st, [&](uint32_t b0, uint32_t b1) {
+                                     Carve c = scratch;  // chunks run one after another on st
+                                     return real_forward_dev(plan, din + n * b0, dout + size_t(bins) * b0,
+                                                             b1 - b0, bins, expand, c, st);
+                                 });
+    }
     if (hin) {
         void* s = cv.take(ib);
         cudaMemcpyAsync(s, fin, ib, cudaMemcpyHostToDevice, st);
         din = static_cast<const real_t*>(s);
     }
     if (hout) dout = static_cast<vec2_t*>(cv.take(ob));
-    if (!real_forward_dev(plan, din, dout, batch, bins,
-                          (plan->flags & KFFT_FLAG_EXPAND_SCALAR) ? 1 : 0, cv, st))
+    if (!real_forward_dev(plan, din, dout, batch, bins, expand, cv, st))
         return KFFT_RET_BUFFER_FAIL;
     if (hout) cudaMemcpyAsync(fout, dout, ob, cudaMemcpyDeviceToHost, st);
     return finish(st);
@@ -829,6 +899,21 @@ KFFT_API kfft_return_t kfft_evali_scalar_batch(kfft_plan_sclr* plan, const kfft_
     if (need && !cv.base) return KFFT_RET_BUFFER_FAIL;  // nothing to carve: no buffer needed
     const vec2_t* din = reinterpret_cast<const vec2_t*>(fin);
     real_t* dout = reinterpret_cast<real_t*>(fout);
+    const uint32_t chunks = ((hin || hout) && !(hin && hout && ranges_overlap(fin, ib, fout, ob)))
+                                ? host_chunks(std::max(ib, ob), batch) : 1;
+    if (chunks > 1) {
+        if (hin) din = static_cast<const vec2_t*>(cv.take(ib));
+        if (hout) dout = static_cast<real_t*>(cv.take(ob));
+        Carve scratch = cv;
+        const size_t n = plan->nfft;
+        return chunked_host_call(batch, chunks, sizeof(vec2_t) * bins, sizeof(real_t) * n,
+                                 hin ? fin : nullptr, const_cast<vec2_t*>(din),
+                                 hout ? fout : nullptr, dout, st, [&](uint32_t b0, uint32_t b1) {
+                                     Carve c = scratch;  // chunks run one after another on st
+                                     return real_inverse_dev(plan, din + size_t(bins) * b0, bins,
+                                                             dout + n * b0, b1 - b0, c, st);
+                                 });
+    }
     if (hin) {
         void* s = cv.take(ib);
         cudaMemcpyAsync(s, fin, ib, cudaMemcpyHostToDevice, st);

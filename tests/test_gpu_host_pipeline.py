@@ -160,3 +160,38 @@ def test_2d_rows_through_bulk_copies(libf):
         assert rel_l2(od.cpu().numpy(), np.fft.fft2(a.astype(np.complex128))) <= TOL32
     finally:
         libf.cleanup(p)
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 16, 300),   # 78 MB in: split into chunks; 262152-byte spectra
+                                     (4095, 5000)])    # odd length: full complex transforms, 80 MB in
+def test_chunked_host_real_batch_matches_device_path(libf, n, batch):
+    """Real forward and inverse batches with host buffers run in overlapping
+    chunks whose copies start on 256-byte boundaries; results equal the
+    device-buffer path bit for bit."""
+    rng = np.random.default_rng(23)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    bins = n if n % 2 else n // 2 + 1  # an odd length gives all n bins, as in the reference
+    fwd = libf.L.kfft_config_scalar(n, 0, None, None)
+    inv = libf.L.kfft_config_scalar(n, K.FLAG_INVERSE, None, None)
+    assert fwd and inv, libf.last_error()
+    try:
+        xd = torch.from_numpy(x).cuda()
+        Xd = torch.empty((batch, bins), dtype=torch.complex64, device="cuda")
+        yd = torch.empty_like(xd)
+        torch.cuda.synchronize()
+        assert libf.L.kfft_eval_scalar_batch(fwd, xd.data_ptr(), Xd.data_ptr(), batch) == 0
+        assert libf.L.kfft_evali_scalar_batch(inv, Xd.data_ptr(), yd.data_ptr(), batch) == 0
+        torch.cuda.synchronize()
+        X_ref, y_ref = Xd.cpu().numpy(), yd.cpu().numpy()
+        X = np.zeros((batch, bins), dtype=np.complex64)
+        y = np.zeros_like(x)
+        assert libf.L.kfft_eval_scalar_batch(fwd, x.ctypes.data, X.ctypes.data, batch) == 0
+        assert libf.L.kfft_evali_scalar_batch(inv, X_ref.ctypes.data, y.ctypes.data, batch) == 0
+        assert np.array_equal(X, X_ref)
+        assert np.array_equal(y, y_ref)
+        spectrum = np.fft.fft if n % 2 else np.fft.rfft
+        for b in (0, batch // 3, batch - 1):
+            assert rel_l2(X[b], spectrum(x[b].astype(np.float64))) <= TOL32
+    finally:
+        libf.cleanup(fwd)
+        libf.cleanup(inv)
