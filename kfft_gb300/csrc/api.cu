@@ -283,7 +283,7 @@ CopyStreams* copy_streams() {
 // Number of chunks a host-buffer batch of `bytes` in `batch` sequences is
 // split into so that its copies overlap the transform (1: no split).
 uint32_t host_chunks(size_t bytes, uint32_t batch) {
-    constexpr size_t kChunkBytes = size_t(16) << 20;
+    constexpr size_t kChunkBytes = size_t(4) << 20;
     if (batch < 2 || bytes < 4 * kChunkBytes) return 1;
     size_t k = bytes / kChunkBytes;
     if (k > 16) k = 16;
