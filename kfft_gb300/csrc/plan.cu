@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -379,6 +380,46 @@ FftPlan::~FftPlan() {
 // ---------------------------------------------------------------------------
 // plan construction
 // ---------------------------------------------------------------------------
+// FP32 powers of two (compile-time bodies): the pass lengths 16..rmax (at
+// most 1024), longest first, with the least estimated time.  A pass costs its
+// measured launch time relative to a 256-point pass on 2^24 points: up to 256
+// points 1 (tiles of 16+ lanes, row segments of 128 bytes or more), 512
+// points 1.44 and 1024 points 1.65 (8 and 4 lanes per 4096-point tile, 16 and
+// 8 on the wide kernel).  Ties go to fewer passes, then to the more even
+// split (lexicographically smaller lengths, longest first).  2^18 runs as 1024 x 256 (0.292 ms per forward + inverse
+// step at 64 sequences, against 0.315 as 512 x 512), 2^20 as 128 x 128 x 64.
+static std::vector<uint32_t> pow2_split(uint32_t N, uint32_t rmax) {
+    uint32_t L = 0;
+    while ((1u << L) < N) ++L;
+    uint32_t emax = 0;
+    while (emax < 10 && (2u << emax) <= rmax) ++emax;
+    auto cost = [](uint32_t e) { return e == 10 ? 1.65 : (e == 9 ? 1.44 : 1.0); };
+    std::vector<uint32_t> best, cur;
+    double best_cost = -1.0;
+    // non-increasing exponents in [4, emax] summing to L
+    std::function<void(uint32_t, uint32_t, double)> walk = [&](uint32_t left, uint32_t top, double c) {
+        if (left == 0) {
+            const bool better = best_cost < 0.0 || c < best_cost - 1e-9 ||
+                                (c < best_cost + 1e-9 && (cur.size() < best.size() ||
+                                                          (cur.size() == best.size() && cur < best)));
+            if (better) {
+                best_cost = c;
+                best = cur;
+            }
+            return;
+        }
+        for (uint32_t e = std::min(top, left); e >= 4; --e) {
+            cur.push_back(e);
+            walk(left - e, e, c + cost(e));
+            cur.pop_back();
+        }
+    };
+    if (emax >= 4) walk(L, emax, 0.0);
+    std::vector<uint32_t> Rs;
+    for (uint32_t e : best) Rs.push_back(1u << e);
+    return Rs;
+}
+
 static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     const uint32_t N = P->N;
     std::vector<uint32_t> Rs;
@@ -397,28 +438,14 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
 #else
         const bool pow2 = false;
 #endif
-        double best = -1.0;
+        if (pow2) Rs = pow2_split(N, V.rmax);
         for (uint32_t rmax : {1024u, 768u, 512u, 384u, 256u, 128u, 64u, 32u, 16u}) {
+            if (!Rs.empty()) break;
             if (rmax > V.rmax) continue;
             std::vector<uint32_t> cand = split_passes(N, rmax);
             bool ok = !cand.empty();
             for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R));
-            if (!ok) continue;
-            if (!pow2) {
-                Rs = cand;
-                break;
-            }
-            // FP32 powers of two (compile-time bodies): the split with the
-            // least estimated time, a pass of up to 256 points counting 1 and
-            // each doubling beyond it 0.5 more (its tiles hold fewer lanes,
-            // so its row segments are narrower: 64 bytes at 512 points, 32 at
-            // 1024); ties go to fewer passes
-            double cost = 0.0;
-            for (uint32_t R : cand) cost += R <= 256 ? 1.0 : 1.0 + 0.5 * std::log2(R / 256.0);
-            if (best < 0.0 || cost < best - 1e-9) {
-                best = cost;
-                Rs = cand;
-            }
+            if (ok) Rs = cand;
         }
     }
     if (Rs.empty()) {
