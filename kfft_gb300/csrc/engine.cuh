@@ -178,6 +178,8 @@ struct PassSpec {
 struct DeviceArena;  // device memory owned by a plan tree
 
 // Planner knobs one plan variant fixes (the tuner's search space).
+// Largest pass length of variant 0's multi-pass splits (a build-time knob for
+// sweeps; variants 1 and 2 lower it to 512 and 256).
 #ifndef KFFT_PLAN_RMAX
 #define KFFT_PLAN_RMAX 1024
 #endif

@@ -241,6 +241,10 @@ kfft_return_t launch(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2
 
 // Contiguous groups of about equal points for the host-buffer path: copies
 // of one group overlap the transform of its neighbours.
+// Host-buffer calls split the batch into at most KFFT_UNEVEN_GROUPS groups
+// of at least 2^KFFT_UNEVEN_GROUP_LOG2 points (measured on the default uneven
+// batch: 8 groups 18.9 ms per e2e step, 16 18.2, 32 17.9, 64 30.3, before the
+// copies were aligned; 16 keeps the recorded graphs few).
 #ifndef KFFT_UNEVEN_GROUPS
 #define KFFT_UNEVEN_GROUPS 16
 #endif
