@@ -325,8 +325,8 @@ kfft_return_t chunked_host_call(uint32_t batch, uint32_t chunks, size_t in_per, 
     EventSet evs;
     const size_t tin = in_per * batch, tout = out_per * batch;
     for (uint32_t k = 0; k < chunks; ++k) {
-        const uint32_t b0 = uint32_t(uint64_t(batch) * k / chunks);
-        const uint32_t b1 = uint32_t(uint64_t(batch) * (k + 1) / chunks);
+        const uint32_t b0 = uint32_t(chunk_start(k, chunks, batch));
+        const uint32_t b1 = uint32_t(chunk_start(k + 1, chunks, batch));
         const bool first = k == 0, last = k + 1 == chunks;
         if (h_in) {
             const CopyRange cr = copy_range(in_per * b0, in_per * b1, tin, first, last);
@@ -628,8 +628,8 @@ KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* 
         EventSet evs;
         const size_t per = sizeof(vec2_t) * size_t(P.N);
         for (uint32_t k = 0; k < chunks; ++k) {
-            const uint32_t b0 = uint32_t(uint64_t(batch) * k / chunks);
-            const uint32_t b1 = uint32_t(uint64_t(batch) * (k + 1) / chunks);
+            const uint32_t b0 = uint32_t(chunk_start(k, chunks, batch));
+            const uint32_t b1 = uint32_t(chunk_start(k + 1, chunks, batch));
             const size_t off = size_t(b0) * P.N;
             const CopyRange cr = copy_range(per * b0, per * b1, bytes, k == 0, k + 1 == chunks);
             if (hin) {

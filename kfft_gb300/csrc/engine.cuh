@@ -256,6 +256,22 @@ bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t*
                   const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
 // Descriptor of pass `pass` of a DIRECT plan (no fused element operations).
+// Start of chunk i (i = 0..k; chunk k's start is `total`) when `total` units
+// are split into k chunks for a host-buffer pipeline: the first and last
+// chunks get a quarter of the share of the others, because the copy in of
+// the first and the transform and copy out of the last overlap nothing.
+// Starts strictly increase when total >= 2k.
+inline uint64_t chunk_start(uint64_t i, uint64_t k, uint64_t total) {
+    if (i == 0) return 0;
+    if (i >= k) return total;
+    if (k < 3 || total < 2 * k) return total * i / k;
+    // weights 1/4, 1, ..., 1, 1/4 in quarters: 1, 4, ..., 4, 1
+    const uint64_t quarters = 4 * (k - 2) + 2;
+    const uint64_t before = 1 + 4 * (i - 1);
+    uint64_t s = total * before / quarters;
+    return s < i ? i : s;
+}
+
 // Copy ranges of a chunked host-buffer call on 256-byte boundaries: copies
 // that start or end off a 128-byte boundary cut the host link's two-way
 // throughput from about 338 to 250 GB/s on this hardware.  The copy in of a

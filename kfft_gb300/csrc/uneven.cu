@@ -260,7 +260,7 @@ void make_groups(kfft_plan_uneven* P) {
     size_t s = 0;
     for (uint64_t g = 0; g < k && s < count; ++g) {
         const size_t s0 = s;
-        const uint64_t target = P->total * (g + 1) / k;
+        const uint64_t target = chunk_start(g + 1, k, P->total);
         if (g + 1 == k) s = count;
         while (s < count && (s == s0 || P->offsets[s] + P->lengths[s] <= target)) ++s;
         ranges.push_back({s0, s});
