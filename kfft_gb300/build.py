@@ -24,7 +24,7 @@ LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 SOURCES = ["pass_smem.cu", "pass_reg.cu", "persistent.cu", "tables.cu", "plan.cu", "api.cu",
            "uneven.cu", "noalloc.cu", "helpers.cu", "mlp.cu"]
-HEADERS = ["engine.cuh", "fft_device.cuh"]
+HEADERS = ["engine.cuh", "fft_device.cuh", "plan_host.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libkfft_gb300.so": [], "libkfft_gb300_f.so": ["-DKFFT_HALF_SCALAR"]}
 

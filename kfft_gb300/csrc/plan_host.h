@@ -1,0 +1,187 @@
+// plan_host.h -- host-only planning arithmetic shared by the planner and its
+// CPU tests: prime factors, the inner radix schedule of a tile, the split of
+// a power-of-two length into passes, and the shared-memory bank model that
+// picks the lane stride of a register tile.  No device code; builds with the
+// host compiler.
+#pragma once
+
+#include <algorithm>
+#include <functional>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace kfft {
+
+inline std::vector<uint32_t> prime_factors(uint32_t n) {
+    std::vector<uint32_t> f;
+    for (uint32_t p = 2; uint64_t(p) * p <= n; ++p)
+        while (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        }
+    if (n > 1) f.push_back(n);
+    return f;
+}
+
+// inner radix schedule of a tile length R: 16s first, then 8/4/2, then odd primes
+inline std::vector<uint8_t> inner_radices(uint32_t R) {
+    std::vector<uint8_t> r;
+    uint32_t e2 = 0;
+    while (R % 2 == 0) {
+        R /= 2;
+        ++e2;
+    }
+    while (e2 >= 4) {
+        r.push_back(16);
+        e2 -= 4;
+    }
+    if (e2 == 3) r.push_back(8);
+    if (e2 == 2) r.push_back(4);
+    if (e2 == 1) r.push_back(2);
+    for (uint32_t p : prime_factors(R)) r.push_back(uint8_t(p));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory lane stride of the register-tile bodies
+// ---------------------------------------------------------------------------
+// Elements per 128-byte shared-memory row (one request of a warp-wide access).
+constexpr uint32_t kRowElems = 128 / sizeof(vec2_t);
+
+// Shared-memory wavefronts of one warp-wide access to the element slots `idx`
+// (-1: thread idle): every kRowElems threads form one request, which takes as
+// many wavefronts as the most distinct elements that share a bank group
+// (slot mod kRowElems).
+inline uint32_t smem_wavefronts(const int64_t* idx) {
+    uint32_t total = 0;
+    for (uint32_t h = 0; h < 32; h += kRowElems) {
+        int64_t seen[kRowElems];
+        uint32_t n = 0;
+        uint32_t per[kRowElems] = {0};
+        for (uint32_t t = h; t < h + kRowElems; ++t) {
+            if (idx[t] < 0) continue;
+            bool dup = false;
+            for (uint32_t i = 0; i < n; ++i) dup = dup || seen[i] == idx[t];
+            if (dup) continue;
+            seen[n++] = idx[t];
+            ++per[idx[t] % kRowElems];
+        }
+        uint32_t worst = 0;
+        for (uint32_t v : per) worst = std::max(worst, v);
+        total += worst;
+    }
+    return total;
+}
+
+// Wavefronts of the shared-memory accesses of one tile iteration of a
+// register-tile body (inner radices of R, C lanes `stride` slots apart, run
+// by `threads` threads).  Stages with a global access in lane mode put
+// consecutive threads on consecutive lanes; the others put them on
+// consecutive butterflies of one lane.
+inline uint64_t tile_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool load_lane,
+                               bool store_lane, uint32_t threads) {
+    auto padh = [](uint64_t i) { return i + i / kRowElems; };
+    const std::vector<uint8_t> rad = inner_radices(R);
+    const size_t np = rad.size();
+    uint64_t cost = 0;
+    uint32_t NS = 1;
+    int64_t idx[32];
+    for (size_t st = 0; st < np; ++st) {
+        const uint32_t P = rad[st], M = R / P, items = C * M;
+        const bool last = st + 1 == np;
+        const bool cfast = (st == 0 && load_lane) || (last && store_lane);
+        const uint32_t warps = std::min<uint32_t>(threads / 32, (items + 31) / 32);
+        for (uint32_t w = 0; w < warps; ++w) {
+            for (uint32_t q = 0; q < P; ++q) {
+                for (int rw = 0; rw < 2; ++rw) {
+                    if ((rw == 0 && st == 0) || (rw == 1 && last)) continue;
+                    for (uint32_t t = 0; t < 32; ++t) {
+                        const uint32_t it = w * 32 + t;
+                        if (it >= items) {
+                            idx[t] = -1;
+                            continue;
+                        }
+                        uint32_t c, jj;
+                        if (cfast) {
+                            jj = it / C;
+                            c = it % C;
+                        } else {
+                            c = it / M;
+                            jj = it % M;
+                        }
+                        const uint64_t ob = uint64_t(jj / NS) * NS * P + jj % NS;
+                        const uint64_t slot = rw == 0 ? padh(jj + uint64_t(q) * M) : padh(ob + uint64_t(q) * NS);
+                        idx[t] = int64_t(uint64_t(c) * stride + slot);
+                    }
+                    cost += smem_wavefronts(idx);
+                }
+            }
+        }
+        NS *= P;
+    }
+    return cost;
+}
+
+// The padded lane length plus the skew (0 .. kRowElems-1 slots) with the
+// fewest shared-memory wavefronts per tile: without a skew the lanes of a
+// lane-major access can all fall in the same banks (a lane of 2^k >= 16
+// points is a whole number of 128-byte rows).  Ties go to the smaller skew.
+inline uint32_t lane_stride_search(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
+                                   uint32_t threads) {
+    const uint32_t base = R + R / kRowElems;
+    uint32_t best = base;
+    uint64_t best_cost = ~uint64_t(0);
+    if (C > 1 && inner_radices(R).size() > 1) {
+        for (uint32_t skew = 0; skew < kRowElems; ++skew) {
+            const uint64_t c = tile_smem_cost(R, C, base + skew, load_lane, store_lane, threads);
+            if (c < best_cost) {
+                best_cost = c;
+                best = base + skew;
+            }
+        }
+    }
+    return best;
+}
+
+// FP32 powers of two (compile-time bodies): the pass lengths 16..rmax (at
+// most 1024), longest first, with the least estimated time.  A pass costs its
+// measured launch time relative to a 256-point pass on 2^24 points: up to 256
+// points 1 (tiles of 16+ lanes, row segments of 128 bytes or more), 512
+// points 1.44 and 1024 points 1.65 (8 and 4 lanes per 4096-point tile, 16 and
+// 8 on the wide kernel).  Ties go to fewer passes, then to the more even
+// split (lexicographically smaller lengths, longest first).  2^18 runs as 1024 x 256 (0.292 ms per forward + inverse
+// step at 64 sequences, against 0.315 as 512 x 512), 2^20 as 128 x 128 x 64.
+inline std::vector<uint32_t> pow2_split(uint32_t N, uint32_t rmax) {
+    uint32_t L = 0;
+    while ((1u << L) < N) ++L;
+    uint32_t emax = 0;
+    while (emax < 10 && (2u << emax) <= rmax) ++emax;
+    auto cost = [](uint32_t e) { return e == 10 ? 1.65 : (e == 9 ? 1.44 : 1.0); };
+    std::vector<uint32_t> best, cur;
+    double best_cost = -1.0;
+    // non-increasing exponents in [4, emax] summing to L
+    std::function<void(uint32_t, uint32_t, double)> walk = [&](uint32_t left, uint32_t top, double c) {
+        if (left == 0) {
+            const bool better = best_cost < 0.0 || c < best_cost - 1e-9 ||
+                                (c < best_cost + 1e-9 && (cur.size() < best.size() ||
+                                                          (cur.size() == best.size() && cur < best)));
+            if (better) {
+                best_cost = c;
+                best = cur;
+            }
+            return;
+        }
+        for (uint32_t e = std::min(top, left); e >= 4; --e) {
+            cur.push_back(e);
+            walk(left - e, e, c + cost(e));
+            cur.pop_back();
+        }
+    };
+    if (emax >= 4) walk(L, emax, 0.0);
+    std::vector<uint32_t> Rs;
+    for (uint32_t e : best) Rs.push_back(1u << e);
+    return Rs;
+}
+
+}  // namespace kfft

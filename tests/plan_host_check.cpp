@@ -1,0 +1,30 @@
+// Prints the host planning arithmetic of plan_host.h (FP32 build) for the
+// CPU test tests/test_plan_host.py: power-of-two pass splits and the lane
+// strides the shared-memory bank model picks, with their wavefront costs.
+#include "plan_host.h"
+
+#include <cstdio>
+
+int main() {
+    for (uint32_t L = 13; L <= 28; ++L)
+        for (uint32_t rmax : {1024u, 512u, 256u}) {
+            std::printf("split %u %u", L, rmax);
+            for (uint32_t R : kfft::pow2_split(1u << L, rmax)) std::printf(" %u", R);
+            std::printf("\n");
+        }
+    const uint32_t cases[][5] = {
+        {512, 8, 1, 0, 256}, {512, 8, 1, 1, 256}, {1024, 4, 1, 1, 256}, {256, 16, 1, 1, 256},
+        {256, 16, 1, 0, 256}, {128, 32, 1, 1, 256}, {64, 64, 1, 1, 256}, {64, 32, 0, 0, 256},
+        {4096, 1, 0, 0, 256}, {2048, 2, 0, 0, 256}, {512, 16, 1, 1, 512}, {1024, 8, 1, 0, 512},
+        {1000, 4, 1, 1, 256}, {768, 5, 1, 0, 256}, {390, 10, 1, 1, 256}, {616, 6, 1, 0, 256}};
+    for (const auto& c : cases) {
+        const uint32_t R = c[0], C = c[1], T = c[4];
+        const bool ll = c[2] != 0, sl = c[3] != 0;
+        const uint32_t s = kfft::lane_stride_search(R, C, ll, sl, T);
+        const uint32_t base = R + R / kfft::kRowElems;
+        std::printf("stride %u %u %u %u %u %u %llu %llu\n", R, C, c[2], c[3], T, s,
+                    (unsigned long long)kfft::tile_smem_cost(R, C, s, ll, sl, T),
+                    (unsigned long long)kfft::tile_smem_cost(R, C, base, ll, sl, T));
+    }
+    return 0;
+}

@@ -1,0 +1,146 @@
+"""Host planning arithmetic (plan_host.h, FP32 build), built with the host
+compiler and checked on the CPU against an independent restatement here:
+the power-of-two pass splits (a search over pass lengths 16..rmax with
+per-pass costs 1 up to 256 points, 1.44 at 512, 1.65 at 1024; ties to fewer
+passes, then the more even split) and the shared-memory bank model that
+picks a register tile's lane stride (wavefronts per 128-byte request, the
+skew with the fewest)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda"):
+        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
+            return os.path.join(d, "include")
+    return None
+
+
+@pytest.fixture(scope="module")
+def printed(tmp_path_factory):
+    cxx, inc = shutil.which("g++"), _cuda_include()
+    if not cxx or not inc:
+        pytest.skip("needs g++ and the CUDA headers")
+    exe = tmp_path_factory.mktemp("plan_host") / "plan_host_check"
+    subprocess.run([cxx, "-std=c++17", "-O1", "-DKFFT_HALF_SCALAR", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.join(ROOT, "kfft_gb300", "csrc"), "-I", inc,
+                    os.path.join(ROOT, "tests", "plan_host_check.cpp"), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=120).stdout
+    return [line.split() for line in out.splitlines()]
+
+
+# ---- restatement -----------------------------------------------------------
+
+def split(L, rmax):
+    emax = min(10, rmax.bit_length() - 1)
+    cost = {9: 1.44, 10: 1.65}
+    best = [None, None]
+    cur = []
+
+    def walk(left, top, c):
+        if left == 0:
+            b = best
+            if (b[0] is None or c < b[0] - 1e-9 or
+                    (c < b[0] + 1e-9 and (len(cur) < len(b[1]) or (len(cur) == len(b[1]) and cur < b[1])))):
+                best[0], best[1] = c, list(cur)
+            return
+        for e in range(min(top, left), 3, -1):
+            cur.append(e)
+            walk(left - e, e, c + cost.get(e, 1.0))
+            cur.pop()
+
+    walk(L, emax, 0.0)
+    return [1 << e for e in best[1]]
+
+
+def radices(R):
+    r, e2 = [], 0
+    while R % 2 == 0:
+        R //= 2
+        e2 += 1
+    r += [16] * (e2 // 4)
+    if e2 % 4:
+        r.append(1 << (e2 % 4))
+    p = 3
+    while R > 1:
+        while R % p == 0:
+            r.append(p)
+            R //= p
+        p += 2
+    return r
+
+
+def pad(i):
+    return i + i // 16
+
+
+def wavefronts(idx):
+    tot = 0
+    for h in (idx[:16], idx[16:]):
+        slots = {}
+        for x in set(v for v in h if v is not None):
+            slots.setdefault(x % 16, set()).add(x)
+        tot += max((len(v) for v in slots.values()), default=0)
+    return tot
+
+
+def cost(R, C, stride, load_lane, store_lane, threads):
+    rad = radices(R)
+    tot, NS = 0, 1
+    for s, P in enumerate(rad):
+        M, last = R // P, s == len(rad) - 1
+        items = C * M
+        cfast = (s == 0 and load_lane) or (last and store_lane)
+        for w in range(min(threads // 32, (items + 31) // 32)):
+            maps = []
+            for t in range(32):
+                it = w * 32 + t
+                if it >= items:
+                    maps.append(None)
+                else:
+                    maps.append(divmod(it, C)[::-1] if cfast else divmod(it, M))
+            for q in range(P):
+                if s > 0:
+                    tot += wavefronts([None if m is None else m[0] * stride + pad(m[1] + q * M) for m in maps])
+                if not last:
+                    tot += wavefronts([None if m is None else
+                                       m[0] * stride + pad((m[1] // NS) * NS * P + m[1] % NS + q * NS) for m in maps])
+        NS *= P
+    return tot
+
+
+def test_pow2_splits_match_restatement(printed):
+    rows = [r for r in printed if r[0] == "split"]
+    assert len(rows) == 16 * 3
+    for r in rows:
+        L, rmax = int(r[1]), int(r[2])
+        assert [int(v) for v in r[3:]] == split(L, rmax), r
+    got = {(int(r[1]), int(r[2])): [int(v) for v in r[3:]] for r in rows}
+    assert got[(18, 1024)] == [1024, 256]
+    assert got[(20, 1024)] == [128, 128, 64]
+    assert got[(24, 1024)] == [256, 256, 256]
+
+
+def test_lane_strides_match_restatement(printed):
+    rows = [r for r in printed if r[0] == "stride"]
+    assert len(rows) == 16
+    for r in rows:
+        R, C, ll, sl, T, s, c_best, c_base = (int(v) for v in r[1:])
+        base = pad(R)
+        costs = [cost(R, C, base + k, ll, sl, T) for k in range(16)]
+        if C > 1 and len(radices(R)) > 1:
+            assert s == base + costs.index(min(costs)), r
+        else:
+            assert s == base
+        assert c_best == cost(R, C, s, ll, sl, T) and c_base == costs[0], r
+        assert c_best <= c_base
+    # the lane-major multi-lane cases the skew exists for
+    by = {(int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5])): (int(r[7]), int(r[8])) for r in rows}
+    assert by[(512, 8, 1, 1, 256)][0] * 2 < by[(512, 8, 1, 1, 256)][1]
+    assert by[(64, 64, 1, 1, 256)][0] * 2 < by[(64, 64, 1, 1, 256)][1]
