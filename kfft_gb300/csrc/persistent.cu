@@ -10,17 +10,23 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
     const int32_t* __restrict__ deps, const QueueItem* __restrict__ items, uint32_t nitems,
     uint32_t* head, uint32_t* done, uint32_t* error, uint32_t max_polls) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_next;
     __shared__ uint32_t s_ok;
     __shared__ __align__(16) PassDesc s_desc;
     vec2_t* buf = reinterpret_cast<vec2_t*>(smem_raw);
+    // Each CTA claims its next item while the current one runs, so the
+    // claim's round trip to L2 overlaps work.  This cannot deadlock: the item
+    // of least queue position among those claimed and not finished has every
+    // dependency (an earlier position) done or in a run of its own.
+    if (threadIdx.x == 0) s_next = atomicAdd(head, 1u);
+    __syncthreads();
     while (true) {
-        if (threadIdx.x == 0) s_item = atomicAdd(head, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
+        const uint32_t it = s_next;
+        __syncthreads();  // every thread has read s_next before it changes
         if (it >= nitems) return;
         const QueueItem q = items[it];
         if (threadIdx.x == 0) {
+            s_next = atomicAdd(head, 1u);
             bool ok = true;
             const int32_t dep = deps[q.desc];
             if (dep >= 0) ok = wait_for(&done[dep], descs[dep].tiles, max_polls);
