@@ -38,7 +38,6 @@ constexpr uint32_t kMultiLanes = 8;   // 64-byte row segments
 constexpr uint32_t kPadShiftHost = 3;
 constexpr uint32_t kMultiLanes = 4;   // 64-byte row segments
 #endif
-constexpr uint32_t kMultiRmax = 1024;
 
 // Multi-lane tiles of passes of 256 points or more hold half a full tile in
 // the FP64 build (measured faster there); FP32 tiles are full (with lanes
@@ -128,16 +127,6 @@ static uint32_t primitive_root(uint32_t p) {
 }
 
 // smallest 7-smooth integer >= n
-static uint64_t next_smooth(uint64_t n) {
-    uint64_t best = UINT64_MAX;
-    for (uint64_t a = 1; a < 2 * n + 2; a *= 2)
-        for (uint64_t b = a; b < 2 * n + 2; b *= 3)
-            for (uint64_t c = b; c < 2 * n + 2; c *= 5)
-                for (uint64_t d = c; d < 2 * n + 2; d *= 7)
-                    if (d >= n && d < best) best = d;
-    return best;
-}
-
 // lanes of a multi-pass register-resident tile
 constexpr uint32_t kRegLanes = 4;
 
@@ -151,71 +140,6 @@ static bool reg_tile_fits(uint32_t R, uint32_t C) {
     for (uint8_t r : rad)
         if (r > 16) return false;
     return true;
-}
-
-// split a DIRECT length into pass lengths, balanced, each <= rmax
-static std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
-    std::vector<uint32_t> f = prime_factors(N);
-    std::sort(f.rbegin(), f.rend());
-    for (uint32_t m = 1; m <= 32; ++m) {
-        std::vector<uint64_t> g(m, 1);
-        bool ok = true;
-        for (uint32_t p : f) {
-            // place in the group with the smallest product that still fits
-            int best = -1;
-            for (uint32_t i = 0; i < m; ++i)
-                if (g[i] * p <= rmax && (best < 0 || g[i] < g[best])) best = int(i);
-            if (best < 0) {
-                ok = false;
-                break;
-            }
-            g[best] *= p;
-        }
-        if (ok) {
-            std::vector<uint32_t> out;
-            for (uint64_t v : g)
-                if (v > 1) out.push_back(uint32_t(v));
-            std::sort(out.rbegin(), out.rend());
-            if (out.empty()) out.push_back(1);
-            return out;
-        }
-    }
-    return {};
-}
-
-// Length of the Bluestein convolution for a minimum of m: the 7-smooth M >= m
-// (up to 2m) with the least estimated cost M * passes(M) * (1 + 0.15 * odd
-// factors).  A pass is one HBM round trip, and radix-3/5/7 stages cost about
-// 30% more per point than radix-2/4/8/16 ones on this kernel; the nearest
-// 7-smooth length is often odd-heavy or one pass deeper than a power-of-two
-// one slightly above it.
-#ifndef KFFT_BLUESTEIN_ODD_COST
-#define KFFT_BLUESTEIN_ODD_COST 0.15
-#endif
-static uint64_t bluestein_length(uint64_t m) {
-    uint64_t best = next_smooth(m);
-    double best_cost = -1.0;
-    for (uint64_t a = 1; a <= 2 * m; a *= 2)
-        for (uint64_t b = a; b <= 2 * m; b *= 3)
-            for (uint64_t c = b; c <= 2 * m; c *= 5)
-                for (uint64_t d = c; d <= 2 * m; d *= 7) {
-                    if (d < m || d > 0xFFFFFFFFull) continue;
-                    uint64_t r = d;
-                    int odd = 0;
-                    for (uint64_t q : {3ull, 5ull, 7ull})
-                        while (r % q == 0) {
-                            r /= q;
-                            ++odd;
-                        }
-                    const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), kMultiRmax).size());
-                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) *
-                                        (1.0 + KFFT_BLUESTEIN_ODD_COST * odd);
-                    if (best_cost < 0 || cost < best_cost) {
-                        best_cost = cost;
-                        best = d;
-                    }
-                }
-    return best;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,11 +1,12 @@
 // plan_host.h -- host-only planning arithmetic shared by the planner and its
-// CPU tests: prime factors, the inner radix schedule of a tile, the split of
-// a power-of-two length into passes, and the shared-memory bank model that
-// picks the lane stride of a register tile.  No device code; builds with the
+// CPU tests: prime factors, the inner radix schedule of a tile, the splits of
+// a length into passes, the Bluestein convolution length, and the
+// shared-memory bank model that picks the lane stride of a register tile.  No device code; builds with the
 // host compiler.
 #pragma once
 
 #include <algorithm>
+#include <cstdint>
 #include <functional>
 #include <vector>
 
@@ -41,6 +42,85 @@ inline std::vector<uint8_t> inner_radices(uint32_t R) {
     if (e2 == 1) r.push_back(2);
     for (uint32_t p : prime_factors(R)) r.push_back(uint8_t(p));
     return r;
+}
+
+// Largest pass length of a balanced multi-pass split.
+constexpr uint32_t kMultiRmax = 1024;
+
+// the least 7-smooth number >= n
+inline uint64_t next_smooth(uint64_t n) {
+    uint64_t best = UINT64_MAX;
+    for (uint64_t a = 1; a < 2 * n + 2; a *= 2)
+        for (uint64_t b = a; b < 2 * n + 2; b *= 3)
+            for (uint64_t c = b; c < 2 * n + 2; c *= 5)
+                for (uint64_t d = c; d < 2 * n + 2; d *= 7)
+                    if (d >= n && d < best) best = d;
+    return best;
+}
+
+// split a DIRECT length into pass lengths, balanced, each <= rmax
+inline std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
+    std::vector<uint32_t> f = prime_factors(N);
+    std::sort(f.rbegin(), f.rend());
+    for (uint32_t m = 1; m <= 32; ++m) {
+        std::vector<uint64_t> g(m, 1);
+        bool ok = true;
+        for (uint32_t p : f) {
+            // place in the group with the smallest product that still fits
+            int best = -1;
+            for (uint32_t i = 0; i < m; ++i)
+                if (g[i] * p <= rmax && (best < 0 || g[i] < g[best])) best = int(i);
+            if (best < 0) {
+                ok = false;
+                break;
+            }
+            g[best] *= p;
+        }
+        if (ok) {
+            std::vector<uint32_t> out;
+            for (uint64_t v : g)
+                if (v > 1) out.push_back(uint32_t(v));
+            std::sort(out.rbegin(), out.rend());
+            if (out.empty()) out.push_back(1);
+            return out;
+        }
+    }
+    return {};
+}
+
+// Length of the Bluestein convolution for a minimum of m: the 7-smooth M >= m
+// (up to 2m) with the least estimated cost M * passes(M) * (1 + 0.15 * odd
+// factors).  A pass is one HBM round trip, and radix-3/5/7 stages cost about
+// 30% more per point than radix-2/4/8/16 ones on this kernel; the nearest
+// 7-smooth length is often odd-heavy or one pass deeper than a power-of-two
+// one slightly above it.
+#ifndef KFFT_BLUESTEIN_ODD_COST
+#define KFFT_BLUESTEIN_ODD_COST 0.15
+#endif
+inline uint64_t bluestein_length(uint64_t m) {
+    uint64_t best = next_smooth(m);
+    double best_cost = -1.0;
+    for (uint64_t a = 1; a <= 2 * m; a *= 2)
+        for (uint64_t b = a; b <= 2 * m; b *= 3)
+            for (uint64_t c = b; c <= 2 * m; c *= 5)
+                for (uint64_t d = c; d <= 2 * m; d *= 7) {
+                    if (d < m || d > 0xFFFFFFFFull) continue;
+                    uint64_t r = d;
+                    int odd = 0;
+                    for (uint64_t q : {3ull, 5ull, 7ull})
+                        while (r % q == 0) {
+                            r /= q;
+                            ++odd;
+                        }
+                    const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), kMultiRmax).size());
+                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) *
+                                        (1.0 + KFFT_BLUESTEIN_ODD_COST * odd);
+                    if (best_cost < 0 || cost < best_cost) {
+                        best_cost = cost;
+                        best = d;
+                    }
+                }
+    return best;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,6 +1,7 @@
 // Prints the host planning arithmetic of plan_host.h (FP32 build) for the
-// CPU test tests/test_plan_host.py: power-of-two pass splits and the lane
-// strides the shared-memory bank model picks, with their wavefront costs.
+// CPU test tests/test_plan_host.py: power-of-two pass splits, the lane
+// strides the shared-memory bank model picks with their wavefront costs,
+// Bluestein convolution lengths and balanced multi-pass splits.
 #include "plan_host.h"
 
 #include <cstdio>
@@ -26,5 +27,13 @@ int main() {
                     (unsigned long long)kfft::tile_smem_cost(R, C, s, ll, sl, T),
                     (unsigned long long)kfft::tile_smem_cost(R, C, base, ll, sl, T));
     }
+    for (uint32_t n : {5u, 17u, 127u, 1009u, 4099u, 65521u, 104729u, 700523u, 999983u})
+        std::printf("bluestein %u %llu\n", n, (unsigned long long)kfft::bluestein_length(2ull * n - 1));
+    for (uint32_t n : {240240u, 1000000u, 729000u, 1081080u, 4096u * 243u})
+        for (uint32_t rmax : {1024u, 512u, 256u}) {
+            std::printf("balanced %u %u", n, rmax);
+            for (uint32_t R : kfft::split_passes(n, rmax)) std::printf(" %u", R);
+            std::printf("\n");
+        }
     return 0;
 }

@@ -2,9 +2,11 @@
 compiler and checked on the CPU against an independent restatement here:
 the power-of-two pass splits (a search over pass lengths 16..rmax with
 per-pass costs 1 up to 256 points, 1.44 at 512, 1.65 at 1024; ties to fewer
-passes, then the more even split) and the shared-memory bank model that
-picks a register tile's lane stride (wavefronts per 128-byte request, the
-skew with the fewest)."""
+passes, then the more even split), the shared-memory bank model that picks a
+register tile's lane stride (wavefronts per 128-byte request, the skew with
+the fewest), the balanced multi-pass split of other lengths, and the
+Bluestein convolution length (the 7-smooth M >= 2N-1, up to twice that,
+with the least M * passes * (1 + 0.15 * odd factors))."""
 import os
 import shutil
 import subprocess
@@ -144,3 +146,77 @@ def test_lane_strides_match_restatement(printed):
     by = {(int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5])): (int(r[7]), int(r[8])) for r in rows}
     assert by[(512, 8, 1, 1, 256)][0] * 2 < by[(512, 8, 1, 1, 256)][1]
     assert by[(64, 64, 1, 1, 256)][0] * 2 < by[(64, 64, 1, 1, 256)][1]
+
+
+def factors(n):
+    f, p = [], 2
+    while p * p <= n:
+        while n % p == 0:
+            f.append(p)
+            n //= p
+        p += 1
+    if n > 1:
+        f.append(n)
+    return f
+
+
+def balanced(n, rmax):
+    f = sorted(factors(n), reverse=True)
+    for m in range(1, 33):
+        g = [1] * m
+        ok = True
+        for p in f:
+            cand = [i for i in range(m) if g[i] * p <= rmax]
+            if not cand:
+                ok = False
+                break
+            i = min(cand, key=lambda i: (g[i], i))
+            g[i] *= p
+        if ok:
+            out = sorted((v for v in g if v > 1), reverse=True)
+            return out or [1]
+    return []
+
+
+def bluestein(m):
+    best, best_cost = None, None
+    a = 1
+    while a <= 2 * m:
+        b = a
+        while b <= 2 * m:
+            c = b
+            while c <= 2 * m:
+                d = c
+                while d <= 2 * m:
+                    if d >= m:
+                        odd, r = 0, d
+                        for q in (3, 5, 7):
+                            while r % q == 0:
+                                r //= q
+                                odd += 1
+                        passes = 1 if d <= 4096 else max(1, len(balanced(d, 1024)))
+                        cost = d * passes * (1.0 + 0.15 * odd)
+                        if best_cost is None or cost < best_cost:
+                            best, best_cost = d, cost
+                    d *= 7
+                c *= 5
+            b *= 3
+        a *= 2
+    return best
+
+
+def test_balanced_splits_match_restatement(printed):
+    rows = [r for r in printed if r[0] == "balanced"]
+    assert len(rows) == 15
+    for r in rows:
+        assert [int(v) for v in r[3:]] == balanced(int(r[1]), int(r[2])), r
+
+
+def test_bluestein_lengths_match_restatement(printed):
+    rows = [r for r in printed if r[0] == "bluestein"]
+    assert len(rows) == 9
+    got = {int(r[1]): int(r[2]) for r in rows}
+    for n, m in got.items():
+        assert m == bluestein(2 * n - 1), (n, m)
+        assert m >= 2 * n - 1
+    assert got[999983] == 1 << 21  # over the nearest 7-smooth length, 2,000,000
