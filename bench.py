@@ -92,6 +92,17 @@ def uneven_lengths(seed=2, count=4096, lo=16, hi=1 << 20, target=1 << 28):
     return out.astype(np.uint32)
 
 
+def uneven_input(total, precision="float", seed=2):
+    """Input of the uneven batch, the same in both arms: re/im iid N(0,1) from
+    numpy's default_rng(seed), drawn in float32 (complex64) or float64."""
+    rng = np.random.default_rng(seed)
+    dt = np.float32 if precision == "float" else np.float64
+    x = np.empty(total, np.complex64 if precision == "float" else np.complex128)
+    x.real = rng.standard_normal(total, dtype=dt)
+    x.imag = rng.standard_normal(total, dtype=dt)
+    return x
+
+
 class Workload:
     name = ""
     precision = "double"
@@ -199,9 +210,9 @@ class Uniform(Workload):
                 "sequences_checked": int(k), "input": self.dist_name}
 
     def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
-        fwd = oracle_mod.CpxPlan(self.N, 0)
-        inv = oracle_mod.CpxPlan(self.N, 1)
-        x = self.host_in.astype(np.complex128)
+        fwd = oracle_mod.CpxPlan(self.N, 0, precision=self.precision)
+        inv = oracle_mod.CpxPlan(self.N, 1, precision=self.precision)
+        x = self.host_in
         n_done, t0 = 0, time.perf_counter()
         while True:
             y = fwd(x, threads)
@@ -395,7 +406,9 @@ class Config4(Workload):
             from concurrent.futures import ThreadPoolExecutor
 
             def row(b):
-                oracle_mod.irfft(oracle_mod.rfft(self.host_in[b % self.B]), self.N)
+                p = self.precision
+                oracle_mod.irfft(oracle_mod.rfft(self.host_in[b % self.B], precision=p), self.N,
+                                 precision=p)
 
             with ThreadPoolExecutor(max_workers=threads) as ex:
                 while time.perf_counter() - t0 < budget_s:
@@ -406,10 +419,10 @@ class Config4(Workload):
             return flops / el / 1e9, f"{calls} rows forward+inverse on {threads} threads, {el:.1f}s", threads
         while time.perf_counter() - t0 < budget_s:
             if self.kind == "c2d":
-                oracle_mod.fft2_cpx(self.host_in)
+                oracle_mod.fft2_cpx(self.host_in, precision=self.precision)
                 flops += 5.0 * self.X * self.Y * math.log2(self.X * self.Y)
             else:
-                oracle_mod.conv2_scalar(self.host_in, self.host_ker)
+                oracle_mod.conv2_scalar(self.host_in, self.host_ker, precision=self.precision)
                 flops += self.flops_per_step()
             calls += 1
         el = time.perf_counter() - t0
@@ -455,11 +468,7 @@ class Uneven(Workload):
                      f" sequences, lengths log-uniform in [16, 2^20], {self.total} points, forward")
 
     def setup(self, torch, dev, nbuf):
-        cdt = torch.complex64 if self.precision == "float" else torch.complex128
-        g = torch.Generator(device="cpu").manual_seed(2)
-        re = torch.randn(self.total, generator=g)
-        im = torch.randn(self.total, generator=g)
-        x = torch.complex(re, im).to(cdt)
+        x = torch.from_numpy(uneven_input(self.total, self.precision))
         self.host_in = x
         self.plan = self.lib.L.kfft_config_cpx_uneven(len(self.lengths), self.lengths.ctypes.data, 0)
         assert self.plan, self.lib.last_error()
@@ -514,27 +523,37 @@ class Uneven(Workload):
         out["against"] = "numpy.fft in FP64, longest sequence of each kind"
         return out
 
-    def cpu_sample(self, oracle_mod, threads, budget_s=8.0):
-        # bounded sample: every 16th sequence of the batch, all host threads,
-        # OpenMP over sequences; repeated until the budget is spent
-        idx = np.arange(0, len(self.lengths), 16)
-        offs = np.concatenate([[0], np.cumsum(self.lengths.astype(np.int64))])
-        x = np.asarray(self.host_in.numpy(), dtype=np.complex128)
-        sub_len = self.lengths[idx]
-        sub = np.concatenate([x[offs[i]:offs[i] + int(self.lengths[i])] for i in idx])
+    def cpu_sample(self, oracle_mod, threads, budget_s=8.0, every=16):
+        """The reference algorithm (oracle port, in the workload's precision)
+        on the host cores, OpenMP over sequences, plans built outside the
+        timer.  every=1 times the whole batch once; every=k > 1 times every
+        k-th sequence, repeated until budget_s is spent."""
+        idx = np.arange(0, len(self.lengths), every)
+        cache = getattr(self, "_cpu_plans", None)
+        if cache is None:
+            cache = self._cpu_plans = {}
+        if every not in cache:  # plans and sample input built once, outside the timer
+            x = np.asarray(self.host_in.numpy())
+            if every == 1:
+                sub_len, sub = self.lengths, x
+            else:
+                offs = np.concatenate([[0], np.cumsum(self.lengths.astype(np.int64))])
+                sub_len = self.lengths[idx]
+                sub = np.concatenate([x[offs[i]:offs[i] + int(self.lengths[i])] for i in idx])
+            cache[every] = (sub_len, sub, oracle_mod.UnevenPlan(sub_len, 0, precision=self.precision))
+        sub_len, sub, plan = cache[every]
         n = sub_len.astype(np.float64)
         flops_call = float(np.sum(5.0 * n * np.log2(np.maximum(n, 2))))
-        plan = oracle_mod.UnevenPlan(sub_len, 0)  # planning is outside the timer
         calls, t0 = 0, time.perf_counter()
         while True:
             plan(sub, threads)
             calls += 1
             el = time.perf_counter() - t0
-            if el > budget_s:
+            if every == 1 or el > budget_s:
                 break
-        plan.close()
-        return flops_call * calls / el / 1e9, (f"every 16th sequence ({len(idx)} of {len(self.lengths)}, "
-                                               f"{int(n.sum())} points) x{calls}, {el:.1f}s")
+        what = ("the whole batch" if every == 1 else
+                f"every {every}th sequence ({len(idx)} of {len(self.lengths)}, {int(n.sum())} points)")
+        return flops_call * calls / el / 1e9, f"{what} x{calls}, {el:.2f}s"
 
 
 # ---------------------------------------------------------------------------
@@ -610,12 +629,30 @@ def dist_env():
     return ws, rank, local
 
 
+def workload_config(wl, ws, nbuf):
+    """The `config` object of both arms' lines (the same workload, the same keys)."""
+    return {"workload": wl.name, "parallelism": f"replicas x{ws}",
+            "l2": "inputs rotate over buffers larger than the 129 MB L2"
+            if nbuf > 1 else "working set larger than the 129 MB L2"}
+
+
+def rotating_buffers(wl):
+    if hasattr(wl, "bytes_per_buffer"):
+        return max(1, int(math.ceil(268e6 / wl.bytes_per_buffer())))
+    return 1
+
+
 def run_reference(args, ws, rank):
-    """The reference algorithm on the host cores (oracle port), same metric."""
+    """The reference algorithm on the host cores: the oracle port in the
+    workload's precision (its float flavour follows the reference's float
+    build, KFFT_HALF_SCALAR), OpenMP over sequences, plans built outside the
+    timer, on the same inputs and for the same metric and config as our arm.
+    The uneven batch is timed whole, one batch per step, when the run fits
+    about four minutes; otherwise every k-th sequence per step, which the
+    line's cpu_baseline.sample states."""
     if rank != 0:
         return
     from oracle import oracle
-    import kfft_gb300  # noqa: F401  (only for the workload definitions' library arg)
 
     class _NoLib:
         L = None
@@ -623,32 +660,50 @@ def run_reference(args, ws, rank):
                        precision=args.precision)
     threads = os.cpu_count() or 1
     if isinstance(wl, Uneven):
-        g = np.random.default_rng(2)
-        x = (g.standard_normal(wl.total) + 1j * g.standard_normal(wl.total)).astype(np.complex64)
         import types
+        x = uneven_input(wl.total, wl.precision)
         wl.host_in = types.SimpleNamespace(numpy=lambda: x)
     elif hasattr(wl, "make_inputs"):
         wl.make_inputs()
     else:
         wl.host_in = wl._input()
-    budget = max(2.0, 20.0 / max(args.steps + args.warmup, 1))
     vals, samples = [], []
-    for _ in range(args.warmup):
-        wl.cpu_sample(oracle, threads, budget_s=budget / 2)
     cores = threads
-    for _ in range(args.steps):
-        res = wl.cpu_sample(oracle, threads, budget_s=budget)
-        vals.append(res[0])
-        samples.append(res[1])
-        if len(res) > 2:
-            cores = res[2]
-    v = statistics.median(vals)
-    ms = wl.flops_per_step() / (v * 1e9) * 1e3
+    if isinstance(wl, Uneven):
+        # first warm-up step: the whole batch (its plans are built before the timer)
+        gf = wl.cpu_sample(oracle, threads, every=1)[0]
+        t_batch = wl.flops_per_step() / (gf * 1e9)
+        runs = args.steps + args.warmup
+        every = 1 if t_batch * runs <= 240.0 else int(math.ceil(t_batch * runs / 240.0))
+        for _ in range(args.warmup - 1):
+            wl.cpu_sample(oracle, threads, budget_s=0.0, every=every)
+        for _ in range(args.steps):
+            res = wl.cpu_sample(oracle, threads, budget_s=0.0, every=every)
+            vals.append(res[0])
+            samples.append(res[1])
+        v = statistics.median(vals)
+        # the whole batch: the median step time; a sample: extrapolated by flops
+        ms = wl.flops_per_step() / (v * 1e9) * 1e3
+    else:
+        budget = max(2.0, 20.0 / max(args.steps + args.warmup, 1))
+        for _ in range(args.warmup):
+            wl.cpu_sample(oracle, threads, budget_s=budget / 2)
+        for _ in range(args.steps):
+            res = wl.cpu_sample(oracle, threads, budget_s=budget)
+            vals.append(res[0])
+            samples.append(res[1])
+            if len(res) > 2:
+                cores = res[2]
+        v = statistics.median(vals)
+        ms = wl.flops_per_step() / (v * 1e9) * 1e3
     line = {"impl": "reference", "metric": "5N*log2N GFLOP/s", "value": round(v, 3),
             "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl.name, "implementation": "reference kfft algorithm (FP64 C oracle port), OpenMP over sequences"},
+            "vs_baseline": None, "dtype": "f32" if wl.precision == "float" else "f64",
+            "data": "synthetic", "config": workload_config(wl, ws, rotating_buffers(wl)),
+            "implementation": (f"reference kfft algorithm (oracle port, "
+                               f"{'float flavour of the float build' if wl.precision == 'float' else 'double build'}),"
+                               f" OpenMP over sequences on {cores} host threads"),
             "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": cores,
                              "kind": "port", "sample": samples[0]},
             "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
@@ -765,9 +820,7 @@ def main():
     probe = make_workload(args.workload, None, subset=args.subset, precision=args.precision)
     lib = kfft_gb300.load(probe.precision)
     wl = make_workload(args.workload, lib, subset=args.subset, precision=args.precision)
-    nbuf = 1
-    if hasattr(wl, "bytes_per_buffer"):
-        nbuf = max(1, int(math.ceil(268e6 / wl.bytes_per_buffer())))
+    nbuf = rotating_buffers(wl)
     wl.setup(torch, dev, nbuf)
     stream = torch.cuda.Stream(device=dev)
     if getattr(wl, "timing_stream_ptr", None) is not None:
@@ -818,9 +871,7 @@ def main():
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if wl.precision == "float" else "f64",
             "data": "synthetic",
-            "config": {"workload": wl.name, "parallelism": f"replicas x{ws}",
-                       "l2": "inputs rotate over buffers larger than the 129 MB L2"
-                       if nbuf > 1 else "working set larger than the 129 MB L2"},
+            "config": workload_config(wl, ws, nbuf),
             "e2e": {"value": round(e2e_val, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
             "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary()}

@@ -25,8 +25,12 @@
  *                                               ext/2d/kfft_scalar2.c:120-246
  *   - circular convolution 1D / 2D           -- ext/conv/kfft_*_conv.c, ext/conv2d/kfft_*_conv.c
  *
- * The oracle always computes in double; a float build of the library is
- * compared against it with a float tolerance.
+ * The oracle computes in double; a float build of the library is compared
+ * against it with a float tolerance.  Compiled with -DORACLE_FLOAT the same
+ * source follows the reference's float build (KFFT_HALF_SCALAR,
+ * incs/kfft_types.h:21-25): data and tables in float (tables computed in
+ * double and rounded once).  That flavour is only the timed CPU baseline of
+ * float workloads, never a checker.
  */
 #include "kfft_oracle.h"
 
@@ -43,6 +47,7 @@
 #define OR_MAX_FACTORS 32
 
 static const double OR_PI = 3.14159265358979323846264338327950288;
+#define OR_HALF ((oreal)0.5)
 
 /* ------------------------------------------------------------------------- */
 /* complex helpers                                                           */
@@ -64,7 +69,7 @@ static inline ocpx csub(ocpx a, ocpx b) {
 static ocpx twiddle(uint32_t k, uint32_t n, int inverse) {
     double phase = -2.0 * OR_PI * (double)k / (double)n;
     if (inverse) phase = -phase;
-    ocpx r = {cos(phase), sin(phase)};
+    ocpx r = {(oreal)cos(phase), (oreal)sin(phase)};
     return r;
 }
 
@@ -248,7 +253,7 @@ static void bfly3(ocpx* F, uint32_t fstride, const oplan* P, uint32_t m) {
         ocpx s2 = cmul(F[u + 2 * m], P->tw[2 * u * fstride]);
         ocpx s3 = cadd(s1, s2);
         ocpx s0 = csub(s1, s2);
-        ocpx a = {F[u].r - 0.5 * s3.r, F[u].i - 0.5 * s3.i};
+        ocpx a = {F[u].r - OR_HALF * s3.r, F[u].i - OR_HALF * s3.i};
         s0.r *= e.i;
         s0.i *= e.i;
         F[u] = cadd(F[u], s3);
@@ -392,12 +397,10 @@ static int plan_exec(const oplan* P, const ocpx* in, ocpx* out) {
     }
     if (ret == OR_RET_SUCCESS && (P->flags & OR_FLAG_INVERSE)) {
         if (P->level > 0 || !(P->flags & OR_FLAG_DISABLE_NORM)) {
-            double s = 1.0 / (double)P->nfft;
             for (uint32_t i = 0; i < P->nfft; i++) {
-                out[i].r = out[i].r / (double)P->nfft;
-                out[i].i = out[i].i / (double)P->nfft;
+                out[i].r = out[i].r / (oreal)P->nfft;
+                out[i].i = out[i].i / (oreal)P->nfft;
             }
-            (void)s;
         }
     }
     return ret;
@@ -524,11 +527,11 @@ int oracle_fft_cpx(uint32_t nfft, uint32_t flags, const ocpx* in, ocpx* out) {
 static ocpx super_twiddle(uint32_t i, uint32_t half, int inverse) {
     double phase = -OR_PI * ((double)(i + 1) / (double)half + 0.5);
     if (inverse) phase = -phase;
-    ocpx r = {cos(phase), sin(phase)};
+    ocpx r = {(oreal)cos(phase), (oreal)sin(phase)};
     return r;
 }
 
-int oracle_rfft(uint32_t nfft, uint32_t flags, const double* in, ocpx* out) {
+int oracle_rfft(uint32_t nfft, uint32_t flags, const oreal* in, ocpx* out) {
     if (flags & OR_FLAG_INVERSE) return OR_RET_IMPROPER_PLAN;
     if (nfft == 0) return OR_RET_SUCCESS;
     uint32_t cflags = flags & ~(uint32_t)OR_FLAG_RENEW;
@@ -557,10 +560,10 @@ int oracle_rfft(uint32_t nfft, uint32_t flags, const double* in, ocpx* out) {
         ocpx fpnk = {z[h - k].r, -z[h - k].i};
         ocpx f1k = cadd(fpk, fpnk), f2k = csub(fpk, fpnk);
         ocpx tw = cmul(f2k, super_twiddle(k - 1, h, 0));
-        out[k].r = 0.5 * (f1k.r + tw.r);
-        out[k].i = 0.5 * (f1k.i + tw.i);
-        out[h - k].r = 0.5 * (f1k.r - tw.r);
-        out[h - k].i = 0.5 * (tw.i - f1k.i);
+        out[k].r = OR_HALF * (f1k.r + tw.r);
+        out[k].i = OR_HALF * (f1k.i + tw.i);
+        out[h - k].r = OR_HALF * (f1k.r - tw.r);
+        out[h - k].i = OR_HALF * (tw.i - f1k.i);
     }
     if (flags & OR_FLAG_EXPAND_SCALAR)
         for (uint32_t k = 1; k < nfft; k++) {
@@ -571,7 +574,7 @@ int oracle_rfft(uint32_t nfft, uint32_t flags, const double* in, ocpx* out) {
     return OR_RET_SUCCESS;
 }
 
-int oracle_irfft(uint32_t nfft, uint32_t flags, const ocpx* in, double* out) {
+int oracle_irfft(uint32_t nfft, uint32_t flags, const ocpx* in, oreal* out) {
     if (!(flags & OR_FLAG_INVERSE)) return OR_RET_IMPROPER_PLAN;
     if (nfft == 0) return OR_RET_SUCCESS;
     uint32_t cflags = flags & ~(uint32_t)OR_FLAG_RENEW;
@@ -646,7 +649,7 @@ int oracle_fft2_cpx(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, ocpx
 }
 
 /* kfft_eval2_scalar, ext/2d/kfft_scalar2.c:120-150 */
-int oracle_rfft2(uint32_t x, uint32_t y, uint32_t flags, const double* in, ocpx* out) {
+int oracle_rfft2(uint32_t x, uint32_t y, uint32_t flags, const oreal* in, ocpx* out) {
     if (flags & OR_FLAG_INVERSE) return OR_RET_IMPROPER_PLAN;
     size_t n = (size_t)x * y;
     if (n == 0) return OR_RET_SUCCESS;
@@ -659,14 +662,14 @@ int oracle_rfft2(uint32_t x, uint32_t y, uint32_t flags, const double* in, ocpx*
 }
 
 /* kfft_evali2_scalar, ext/2d/kfft_scalar2.c:185-246 */
-int oracle_irfft2(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, double* out) {
+int oracle_irfft2(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, oreal* out) {
     if (!(flags & OR_FLAG_INVERSE)) return OR_RET_IMPROPER_PLAN;
     size_t n = (size_t)x * y;
     if (n == 0) return OR_RET_SUCCESS;
     uint32_t cflags = flags & ~(uint32_t)OR_FLAG_RENEW;
     ocpx* rows = (ocpx*)malloc(sizeof(ocpx) * n);
     ocpx* col = (ocpx*)malloc(sizeof(ocpx) * y);
-    double* colr = (double*)malloc(sizeof(double) * (y + 2));
+    oreal* colr = (oreal*)malloc(sizeof(oreal) * (y + 2));
     if (!rows || !col || !colr) {
         free(rows);
         free(col);
@@ -714,8 +717,8 @@ int oracle_conv_cpx(uint32_t nfft, uint32_t flags, const ocpx* a, const ocpx* b,
 }
 
 /* kfft_eval_conv_scalar, ext/conv/kfft_scalar_conv.c:74-100 */
-int oracle_conv_scalar(uint32_t nfft, uint32_t flags, const double* a, const double* b,
-                       double* out) {
+int oracle_conv_scalar(uint32_t nfft, uint32_t flags, const oreal* a, const oreal* b,
+                       oreal* out) {
     uint32_t f = flags & ~(uint32_t)(OR_FLAG_RENEW | OR_FLAG_INVERSE);
     ocpx* A = (ocpx*)calloc(nfft + 1, sizeof(ocpx));
     ocpx* B = (ocpx*)calloc(nfft + 1, sizeof(ocpx));
@@ -759,8 +762,8 @@ int oracle_conv2_cpx(uint32_t x, uint32_t y, uint32_t flags, const ocpx* a, cons
 }
 
 /* kfft_eval2_conv_scalar, ext/conv2d/kfft_scalar_conv.c:79-107 */
-int oracle_conv2_scalar(uint32_t x, uint32_t y, uint32_t flags, const double* a, const double* b,
-                        double* out) {
+int oracle_conv2_scalar(uint32_t x, uint32_t y, uint32_t flags, const oreal* a, const oreal* b,
+                        oreal* out) {
     size_t n = (size_t)x * y;
     uint32_t f = flags & ~(uint32_t)(OR_FLAG_RENEW | OR_FLAG_INVERSE);
     ocpx* A = (ocpx*)malloc(sizeof(ocpx) * (n ? n : 1));
@@ -794,8 +797,8 @@ int oracle_dft_exact(uint32_t nfft, int inverse, const ocpx* in, ocpx* out) {
             sr += (long double)in[n].r * c - (long double)in[n].i * s;
             si += (long double)in[n].r * s + (long double)in[n].i * c;
         }
-        out[k].r = (double)sr;
-        out[k].i = (double)si;
+        out[k].r = (oreal)sr;
+        out[k].i = (oreal)si;
     }
     return OR_RET_SUCCESS;
 }

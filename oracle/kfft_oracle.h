@@ -10,8 +10,18 @@
 extern "C" {
 #endif
 
+/* The default build computes in double.  Compiled with -DORACLE_FLOAT it
+ * follows the reference's float build (KFFT_HALF_SCALAR, incs/kfft_types.h:21-25):
+ * data, butterflies and tables in float, tables computed in double and rounded
+ * once.  The float flavour is the timed CPU baseline of float workloads. */
+#ifdef ORACLE_FLOAT
+typedef float oreal;
+#else
+typedef double oreal;
+#endif
+
 typedef struct {
-    double r, i;
+    oreal r, i;
 } ocpx;
 
 /* flag and return values of the reference, incs/kfft_types.h:46-57, 82-94 */
@@ -44,18 +54,18 @@ int oracle_uneven_exec(const void* u, const ocpx* in, ocpx* out, int threads);
 void oracle_uneven_free(void* u);
 int oracle_exec_uneven(uint32_t count, const uint32_t* lengths, uint32_t flags, const ocpx* in,
                        ocpx* out, int threads);
-int oracle_rfft(uint32_t nfft, uint32_t flags, const double* in, ocpx* out);
-int oracle_irfft(uint32_t nfft, uint32_t flags, const ocpx* in, double* out);
+int oracle_rfft(uint32_t nfft, uint32_t flags, const oreal* in, ocpx* out);
+int oracle_irfft(uint32_t nfft, uint32_t flags, const ocpx* in, oreal* out);
 int oracle_fft2_cpx(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, ocpx* out);
-int oracle_rfft2(uint32_t x, uint32_t y, uint32_t flags, const double* in, ocpx* out);
-int oracle_irfft2(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, double* out);
+int oracle_rfft2(uint32_t x, uint32_t y, uint32_t flags, const oreal* in, ocpx* out);
+int oracle_irfft2(uint32_t x, uint32_t y, uint32_t flags, const ocpx* in, oreal* out);
 int oracle_conv_cpx(uint32_t nfft, uint32_t flags, const ocpx* a, const ocpx* b, ocpx* out);
-int oracle_conv_scalar(uint32_t nfft, uint32_t flags, const double* a, const double* b,
-                       double* out);
+int oracle_conv_scalar(uint32_t nfft, uint32_t flags, const oreal* a, const oreal* b,
+                       oreal* out);
 int oracle_conv2_cpx(uint32_t x, uint32_t y, uint32_t flags, const ocpx* a, const ocpx* b,
                      ocpx* out);
-int oracle_conv2_scalar(uint32_t x, uint32_t y, uint32_t flags, const double* a, const double* b,
-                        double* out);
+int oracle_conv2_scalar(uint32_t x, uint32_t y, uint32_t flags, const oreal* a, const oreal* b,
+                        oreal* out);
 int oracle_dft_exact(uint32_t nfft, int inverse, const ocpx* in, ocpx* out);
 
 #ifdef __cplusplus

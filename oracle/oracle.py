@@ -21,6 +21,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 SO_PATH = os.path.join(BUILD_DIR, "libkfft_oracle.so")
+# float flavour: the same source compiled with -DORACLE_FLOAT, following the
+# reference's float build; only a timed baseline, never a checker
+SO_PATH_F = os.path.join(BUILD_DIR, "libkfft_oracle_f.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 FLAG_NORMAL = 0
@@ -32,29 +35,38 @@ FLAG_EXPAND_SCALAR = 1 << 4
 FLAG_DISABLE_NORM = 1 << 5
 
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 
-def build(force: bool = False) -> str:
-    """Compile the oracle C restatement into oracle/_build (gcc, OpenMP)."""
+def build(force: bool = False, precision: str = "double") -> str:
+    """Compile the oracle C restatement into oracle/_build (gcc, OpenMP); the
+    float flavour with -DORACLE_FLOAT."""
     src = os.path.join(HERE, "kfft_oracle.c")
-    if (not force and os.path.exists(SO_PATH)
-            and os.path.getmtime(SO_PATH) >= os.path.getmtime(src)):
-        return SO_PATH
+    hdr = os.path.join(HERE, "kfft_oracle.h")
+    so = SO_PATH_F if precision == "float" else SO_PATH
+    if (not force and os.path.exists(so)
+            and os.path.getmtime(so) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return so
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = SO_PATH + f".tmp{os.getpid()}"
+    tmp = so + f".tmp{os.getpid()}"
     cmd = ["gcc", "-std=gnu11", "-O3", "-fPIC", "-fopenmp", "-shared", "-o", tmp, src, "-lm"]
+    if precision == "float":
+        cmd.insert(1, "-DORACLE_FLOAT")
     subprocess.run(cmd, check=True)
-    os.replace(tmp, SO_PATH)
-    return SO_PATH
+    os.replace(tmp, so)
+    return so
 
 
-def _load():
-    global _lib
+def build_all(force: bool = False) -> None:
+    build(force, "double")
+    build(force, "float")
+
+
+def _load(precision: str = "double"):
     with _lock:
-        if _lib is not None:
-            return _lib
-        lib = ctypes.CDLL(build())
+        if precision in _libs:
+            return _libs[precision]
+        lib = ctypes.CDLL(build(precision=precision))
         vp, u32, i32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64
         lib.oracle_plan_cpx.restype = vp
         lib.oracle_plan_cpx.argtypes = [u32, u32]
@@ -79,16 +91,16 @@ def _load():
         lib.oracle_uneven_create.argtypes = [u32, vp, u32]
         lib.oracle_uneven_exec.argtypes = [vp, vp, vp, i32]
         lib.oracle_uneven_free.argtypes = [vp]
-        _lib = lib
+        _libs[precision] = lib
         return lib
 
 
-def _c128(a):
-    return np.ascontiguousarray(a, dtype=np.complex128)
+def _c128(a, precision: str = "double"):
+    return np.ascontiguousarray(a, dtype=np.complex64 if precision == "float" else np.complex128)
 
 
-def _f64(a):
-    return np.ascontiguousarray(a, dtype=np.float64)
+def _f64(a, precision: str = "double"):
+    return np.ascontiguousarray(a, dtype=np.float32 if precision == "float" else np.float64)
 
 
 def _check(r, what):
@@ -99,15 +111,16 @@ def _check(r, what):
 class CpxPlan:
     """An oracle complex plan of one length, reusable over a batch."""
 
-    def __init__(self, nfft: int, flags: int = 0):
-        self.lib = _load()
+    def __init__(self, nfft: int, flags: int = 0, precision: str = "double"):
+        self.lib = _load(precision)
+        self.precision = precision
         self.nfft = nfft
         self.ptr = self.lib.oracle_plan_cpx(nfft, flags)
         if not self.ptr:
             raise MemoryError("oracle plan allocation failed")
 
     def __call__(self, x, threads: int = 0):
-        x = _c128(x)
+        x = _c128(x, self.precision)
         batch = x.size // max(self.nfft, 1)
         y = np.empty_like(x)
         _check(self.lib.oracle_exec_cpx_batch(self.ptr, x.ctypes.data, y.ctypes.data,
@@ -126,45 +139,46 @@ class CpxPlan:
             pass
 
 
-def fft_cpx(x, flags: int = 0):
+def fft_cpx(x, flags: int = 0, precision: str = "double"):
     """kfft_eval_cpx on one or more rows (last axis = sequence)."""
-    x = _c128(x)
+    x = _c128(x, precision)
     n = x.shape[-1]
-    p = CpxPlan(n, flags)
+    p = CpxPlan(n, flags, precision)
     try:
         return p(x).reshape(x.shape)
     finally:
         p.close()
 
 
-def rfft(x, flags: int = 0):
-    lib = _load()
-    x = _f64(x)
+def rfft(x, flags: int = 0, precision: str = "double"):
+    lib = _load(precision)
+    x = _f64(x, precision)
     n = x.size
-    out = np.zeros(n if (flags & FLAG_EXPAND_SCALAR or n % 2) else n // 2 + 1, np.complex128)
+    cdt = np.complex64 if precision == "float" else np.complex128
+    out = np.zeros(n if (flags & FLAG_EXPAND_SCALAR or n % 2) else n // 2 + 1, cdt)
     if n % 2 == 0 and not flags & FLAG_EXPAND_SCALAR:
-        buf = np.zeros(n // 2 + 1, np.complex128)
+        buf = np.zeros(n // 2 + 1, cdt)
     else:
-        buf = np.zeros(max(n, n // 2 + 1), np.complex128)
+        buf = np.zeros(max(n, n // 2 + 1), cdt)
     _check(lib.oracle_rfft(n, flags, x.ctypes.data, buf.ctypes.data), "rfft")
     return buf[: out.size].copy()
 
 
-def irfft(X, n: int, flags: int = FLAG_INVERSE):
-    lib = _load()
-    X = _c128(X)
+def irfft(X, n: int, flags: int = FLAG_INVERSE, precision: str = "double"):
+    lib = _load(precision)
+    X = _c128(X, precision)
     need = n if n % 2 else n // 2 + 1
     if X.size < need:
         raise ValueError("spectrum too short")
-    out = np.zeros(n + 2, np.float64)
+    out = np.zeros(n + 2, np.float32 if precision == "float" else np.float64)
     _check(lib.oracle_irfft(n, flags, X.ctypes.data, out.ctypes.data), "irfft")
     return out[:n].copy()
 
 
-def fft2_cpx(a, flags: int = 0):
+def fft2_cpx(a, flags: int = 0, precision: str = "double"):
     """2D complex transform of a (y, x) row-major array (x contiguous)."""
-    lib = _load()
-    a = _c128(a)
+    lib = _load(precision)
+    a = _c128(a, precision)
     y, x = a.shape
     out = np.empty_like(a)
     _check(lib.oracle_fft2_cpx(x, y, flags, a.ctypes.data, out.ctypes.data), "fft2_cpx")
@@ -217,11 +231,11 @@ def conv2_cpx(a, b, flags: int = 0):
     return out
 
 
-def conv2_scalar(a, b, flags: int = 0):
-    lib = _load()
-    a, b = _f64(a), _f64(b)
+def conv2_scalar(a, b, flags: int = 0, precision: str = "double"):
+    lib = _load(precision)
+    a, b = _f64(a, precision), _f64(b, precision)
     y, x = a.shape
-    out = np.zeros((y, x), np.float64)
+    out = np.zeros((y, x), np.float32 if precision == "float" else np.float64)
     _check(lib.oracle_conv2_scalar(x, y, flags, a.ctypes.data, b.ctypes.data,
                                    out.ctypes.data), "conv2_scalar")
     return out
@@ -243,8 +257,9 @@ def fft_uneven(lengths, x, flags: int = 0, threads: int = 0):
 class UnevenPlan:
     """Oracle plans for a packed batch of uneven lengths, built once."""
 
-    def __init__(self, lengths, flags: int = 0):
-        self.lib = _load()
+    def __init__(self, lengths, flags: int = 0, precision: str = "double"):
+        self.lib = _load(precision)
+        self.precision = precision
         self.lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
         self.total = int(self.lengths.sum(dtype=np.int64))
         self.ptr = self.lib.oracle_uneven_create(self.lengths.size, self.lengths.ctypes.data, flags)
@@ -252,7 +267,7 @@ class UnevenPlan:
             raise MemoryError("oracle uneven plan failed")
 
     def __call__(self, x, threads: int = 0):
-        x = _c128(x)
+        x = _c128(x, self.precision)
         if x.size != self.total:
             raise ValueError("input size does not match the lengths")
         y = np.empty_like(x)
