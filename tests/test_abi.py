@@ -150,3 +150,16 @@ def test_dynapi_callback_types_match_the_functions(tmp_path, half):
         cmd.insert(1, "-DKFFT_HALF_SCALAR")
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("precision", ["double", "float"])
+def test_tiny_api_program_compiles_and_links(tmp_path, precision):
+    """The tiny-API program (include/kfft_tiny.h) builds with -Wall -Werror
+    against either engine build; running it needs a GPU (test_gpu_tiny_api.py)."""
+    from tests.test_gpu_tiny_api import build_tiny_program
+    lib = os.path.join(ROOT, "kfft_gb300", "lib",
+                       "libkfft_gb300.so" if precision == "double" else "libkfft_gb300_f.so")
+    if not os.path.isfile(lib):
+        pytest.skip("engine library not built")
+    exe = build_tiny_program(str(tmp_path), precision)
+    assert os.path.isfile(exe)
