@@ -78,9 +78,15 @@ KFFT_API void kfft_release_uneven(kfft_plan_uneven* plan);
  * passes lives in one file-scope device array of kfft_noalloc_scratch_bytes()
  * bytes (32 MiB) that every GPU loading this library holds until the process
  * exits; requests that need more return KFFT_RET_BADARGUMENTS and
- * kfft_noalloc_last_message() says why.  The first call on each device looks
- * up the array's device address and should be made before any stream capture.
- * All calls share the array: calls whose kernels overlap on the GPU race.
+ * kfft_noalloc_last_message() says why (per host thread; "" after a call that
+ * was not rejected).  The first call on each device looks up the array's
+ * device address and should be made before any stream capture; the first call
+ * with each (plan, batch) shape may also set up the pass kernels it picks
+ * (shared-memory limit, occupancy query, lazy module load), so run every shape
+ * once before a region that must not do that.  All calls share the array:
+ * calls whose kernels overlap on the GPU race.  A bounded bulk-copy wait that
+ * runs out during this asynchronous call is reported by
+ * kfft_gb300_check_waits(stream).
  */
 KFFT_API kfft_return_t kfft_eval_cpx_noalloc(kfft_plan_cpx* plan, const kfft_cpx* fin,
                                              kfft_cpx* fout, uint32_t batch, void* stream);
@@ -150,6 +156,21 @@ KFFT_API kfft_return_t kfft_mlp_train(kfft_mlp* m, const float* X, const float* 
  * 1: a wait gave up and the kernel returned) or -1 on a CUDA error.
  */
 KFFT_API int kfft_gb300_queue_selftest(uint32_t max_polls, int satisfiable);
+
+/*
+ * Bounded device waits.  The FP32 single-pass kernel that receives its tiles
+ * by bulk copy waits on each copy with a bounded poll loop; if a wait runs out
+ * (only a failed or very slow copy can cause that) its CTA stops and the
+ * output is incomplete.  Synchronous entry points then return
+ * KFFT_RET_BUFFER_FAIL.  For asynchronous entry points (kfft_eval_cpx_async,
+ * kfft_eval_cpx_noalloc) kfft_gb300_check_waits synchronises `stream` and
+ * returns 1 if such a wait of this host thread's earlier calls ran out, 0 if
+ * none did, -1 on a CUDA error; it clears the record.
+ * kfft_gb300_set_bulk_wait_polls is a test hook: the polls a wait makes
+ * before it gives up (0 restores the default of about a second).
+ */
+KFFT_API int kfft_gb300_check_waits(void* stream);
+KFFT_API void kfft_gb300_set_bulk_wait_polls(uint32_t polls);
 
 /* Engine introspection (used by tests and the benchmark). */
 typedef struct {

@@ -61,6 +61,7 @@ EXPORTED_SYMBOLS = [
     "kfft_tune_clear",
     "kfft_mlp_create", "kfft_mlp_release", "kfft_mlp_params", "kfft_mlp_get", "kfft_mlp_set",
     "kfft_mlp_predict", "kfft_mlp_loss_grad", "kfft_mlp_train", "kfft_gb300_queue_selftest",
+    "kfft_gb300_check_waits", "kfft_gb300_set_bulk_wait_polls",
 ]
 
 
@@ -198,6 +199,10 @@ class KfftLib:
                                      fp]
         L.kfft_gb300_queue_selftest.restype = ctypes.c_int
         L.kfft_gb300_queue_selftest.argtypes = [u32, ctypes.c_int]
+        L.kfft_gb300_check_waits.restype = ctypes.c_int
+        L.kfft_gb300_check_waits.argtypes = [vp]
+        L.kfft_gb300_set_bulk_wait_polls.restype = None
+        L.kfft_gb300_set_bulk_wait_polls.argtypes = [u32]
         L.kfft_gb300_last_error.restype = ctypes.c_char_p
         L.kfft_gb300_describe.restype = ctypes.c_char_p
         L.kfft_gb300_describe.argtypes = [vp]

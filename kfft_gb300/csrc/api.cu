@@ -15,9 +15,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -53,6 +55,11 @@ void note_cuda_error(cudaError_t e) {
     g_err_text = cudaGetErrorString(e);
 }
 
+void note_engine_error(const char* msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err_text = msg;
+}
+
 bool ensure_device() {
     std::call_once(g_dev_once, [] {
         int n = 0;
@@ -84,20 +91,32 @@ int take_pending_error() {
 // ===========================================================================
 // device plan handle, placed in the plan's pool
 // ===========================================================================
+// One cached device workspace per host thread that evaluates the plan: the
+// plan's tables are read-only, so evaluations of one plan from several host
+// threads run concurrently, each on its own workspace and its own per-thread
+// stream (the reference lets threads share a plan, ext/2d/kfft_cpx2.c:100-104).
+struct WorkspaceSlot {
+    std::thread::id owner;
+    void* ws = nullptr;
+    size_t size = 0;
+};
+
 struct kfft_gpu_plan {
     DeviceArena* arena = nullptr;
     FftPlan* plan = nullptr;      // complex transform (or the basis of a real plan)
     const vec2_t* super_tw = nullptr;  // real transform post/pre twiddles
-    std::mutex* mu = nullptr;
-    void* ws = nullptr;  // cached device workspace
-    size_t ws_size = 0;
+    std::mutex* mu = nullptr;     // guards `slots` (held only to find a slot)
+    std::deque<WorkspaceSlot>* slots = nullptr;  // a deque: slots never move
     void release() {
-        if (ws) {
-            cudaFree(ws);
-            account_device_bytes(-int64_t(ws_size));
+        if (slots) {
+            for (WorkspaceSlot& s : *slots)
+                if (s.ws) {
+                    cudaFree(s.ws);
+                    account_device_bytes(-int64_t(s.size));
+                }
         }
-        ws = nullptr;
-        ws_size = 0;
+        delete slots;
+        slots = nullptr;
         delete plan;
         plan = nullptr;
         delete arena;
@@ -105,14 +124,27 @@ struct kfft_gpu_plan {
         delete mu;
         mu = nullptr;
     }
-    // returns a device workspace of at least `bytes`, growing the cached one
+    // this host thread's device workspace of at least `bytes`, growing its
+    // cached one (only the owning thread ever touches a slot's buffer)
     void* workspace(size_t bytes) {
-        if (bytes <= ws_size) return ws;
-        if (ws) {
-            cudaFree(ws);
-            account_device_bytes(-int64_t(ws_size));
-            ws = nullptr;
-            ws_size = 0;
+        WorkspaceSlot* slot = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(*mu);
+            const std::thread::id me = std::this_thread::get_id();
+            for (WorkspaceSlot& s : *slots)
+                if (s.owner == me) slot = &s;
+            if (!slot) {
+                slots->push_back(WorkspaceSlot());
+                slot = &slots->back();
+                slot->owner = me;
+            }
+        }
+        if (bytes <= slot->size) return slot->ws;
+        if (slot->ws) {
+            cudaFree(slot->ws);
+            account_device_bytes(-int64_t(slot->size));
+            slot->ws = nullptr;
+            slot->size = 0;
         }
         void* p = nullptr;
         cudaError_t e = cudaMalloc(&p, bytes);
@@ -120,10 +152,10 @@ struct kfft_gpu_plan {
             note_cuda_error(e);
             return nullptr;
         }
-        ws = p;
-        ws_size = bytes;
+        slot->ws = p;
+        slot->size = bytes;
         account_device_bytes(int64_t(bytes));
-        return ws;
+        return p;
     }
 };
 
@@ -152,6 +184,7 @@ kfft_gpu_plan* new_gpu_handle(kfft_pool_t* A) {
     if (!mem) return nullptr;
     kfft_gpu_plan* g = new (mem) kfft_gpu_plan();
     g->mu = new std::mutex();
+    g->slots = new std::deque<WorkspaceSlot>();
     g->arena = new DeviceArena();
     if (!A->device) A->device = new PoolRegistry();
     static_cast<PoolRegistry*>(A->device)->plans.push_back(g);
@@ -175,8 +208,10 @@ kfft_return_t finish(cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) note_cuda_error(e);
+    const bool wait_failed = take_wait_failures(st);
+    if (wait_failed) note_engine_error("a bounded bulk-copy wait ran out; the output is incomplete");
     const int pending = take_pending_error();
-    return pending ? KFFT_RET_BUFFER_FAIL : KFFT_RET_SUCCESS;
+    return (pending || wait_failed) ? KFFT_RET_BUFFER_FAIL : KFFT_RET_SUCCESS;
 }
 
 real_t inverse_scale(uint32_t flags, uint32_t n) {
@@ -205,9 +240,28 @@ struct Carve {
 
 size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// A convolution's spectrum product fused into the store of the last pass
+// that writes a spectrum: with `mul` set (a spectrum in the same layout as the
+// output), the last pass's plain store becomes out = v * mul, and *fused
+// tells the caller that no separate product sweep is needed.  Passes whose
+// last store already carries an element operation (Rader, Bluestein) keep it
+// and leave *fused false.
+struct Product {
+    const vec2_t* mul = nullptr;
+    bool* fused = nullptr;
+};
+
+void attach_product(std::vector<PassDesc>& descs, const Product& pr) {
+    if (pr.fused) *pr.fused = false;
+    if (!pr.mul || descs.empty() || descs.back().epi_op != EPI_NONE) return;
+    descs.back().epi_op = EPI_MUL_OUT;
+    descs.back().epi_tab = pr.mul;
+    if (pr.fused) *pr.fused = true;
+}
+
 // Runs the complex transform of `g` on device buffers.
 bool run_cpx(const FftPlan& P, const vec2_t* din, vec2_t* dout, uint32_t batch, real_t scale,
-             void* wsmem, size_t wsbytes, cudaStream_t st) {
+             void* wsmem, size_t wsbytes, cudaStream_t st, const Product& pr = Product()) {
     Workspace ws;
     ws.base = static_cast<char*>(wsmem);
     ws.size = wsbytes;
@@ -216,13 +270,15 @@ bool run_cpx(const FftPlan& P, const vec2_t* din, vec2_t* dout, uint32_t batch, 
     l.bs = P.N;
     std::vector<PassDesc> descs;
     if (!build_passes(P, din, l, dout, l, scale, ws, descs)) return false;
+    attach_product(descs, pr);
     run_passes(descs, st);
     return true;
 }
 
 // Column transform of a (rows=y, cols=x) complex array in place.
 bool run_columns(const FftPlan& Py, vec2_t* data, uint32_t x, uint32_t y, real_t scale,
-                 Carve& cv, cudaStream_t st) {
+                 Carve& cv, cudaStream_t st, const Product& pr = Product()) {
+    if (pr.fused) *pr.fused = false;
     if (Py.method == METHOD_DIRECT) {
         Layout l;
         l.batch = x;
@@ -236,6 +292,7 @@ bool run_columns(const FftPlan& Py, vec2_t* data, uint32_t x, uint32_t y, real_t
         if (wb && !ws.base) return false;
         std::vector<PassDesc> descs;
         if (!build_passes(Py, data, l, data, l, scale, ws, descs)) return false;
+        attach_product(descs, pr);
         run_passes(descs, st);
         return true;
     }
@@ -255,11 +312,6 @@ size_t columns_bytes(const FftPlan& Py, uint32_t x, uint32_t y) {
     if (Py.method == METHOD_DIRECT) return r256(workspace_bytes(Py, x));
     return 2 * r256(sizeof(vec2_t) * size_t(x) * y) + r256(workspace_bytes(Py, x));
 }
-
-struct EvalGuard {
-    std::unique_lock<std::mutex> lk;
-    explicit EvalGuard(kfft_gpu_plan* g) : lk(*g->mu) {}
-};
 
 // Copy streams of this host thread for the chunked host-buffer path: copies
 // in, compute and copies out of successive chunks overlap.
@@ -597,7 +649,6 @@ KFFT_API kfft_return_t kfft_eval_cpx_batch(kfft_plan_cpx* plan, const kfft_cpx* 
     if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->gpu;
     if (!g || !g->plan) return KFFT_RET_IMPROPER_PLAN;
-    EvalGuard guard(g);
     cudaSetDevice(current_device());
     cudaStream_t st = sync_stream();
     const FftPlan& P = *g->plan;
@@ -677,7 +728,6 @@ KFFT_API kfft_return_t kfft_eval_cpx_async(kfft_plan_cpx* plan, const kfft_cpx* 
     if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->gpu;
     if (!g || !g->plan) return KFFT_RET_IMPROPER_PLAN;
-    EvalGuard guard(g);
     cudaSetDevice(current_device());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const FftPlan& P = *g->plan;
@@ -745,7 +795,9 @@ uint32_t real_bins(const kfft_plan_sclr* p) {
 
 // forward real transform on device buffers; spectrum stride `bins`
 bool real_forward_dev(const kfft_plan_sclr* p, const real_t* din, vec2_t* dout, uint32_t batch,
-                      uint64_t out_bs, int expand, Carve& cv, cudaStream_t st) {
+                      uint64_t out_bs, int expand, Carve& cv, cudaStream_t st,
+                      const Product& pr = Product()) {
+    if (pr.fused) *pr.fused = false;
     const uint32_t n = p->nfft;
     const FftPlan& B = *p->basis->gpu->plan;
     if (n % 2) {
@@ -764,6 +816,7 @@ bool real_forward_dev(const kfft_plan_sclr* p, const real_t* din, vec2_t* dout, 
         lo.bs = out_bs;
         std::vector<PassDesc> d;
         if (!build_passes(B, w, li, dout, lo, real_t(1), wsp, d)) return false;
+        attach_product(d, pr);
         run_passes(d, st);
         return true;
     }
@@ -774,7 +827,8 @@ bool real_forward_dev(const kfft_plan_sclr* p, const real_t* din, vec2_t* dout, 
     if (!z || (wb && !ws)) return false;
     if (!run_cpx(B, reinterpret_cast<const vec2_t*>(din), z, batch, real_t(1), ws, wb, st))
         return false;
-    launch_real_post(z, dout, p->gpu->super_tw, h, batch, out_bs, expand, st);
+    launch_real_post(z, dout, p->gpu->super_tw, h, batch, out_bs, expand, st, pr.mul);
+    if (pr.fused && pr.mul) *pr.fused = true;
     return true;
 }
 
@@ -831,7 +885,6 @@ KFFT_API kfft_return_t kfft_eval_scalar_batch(kfft_plan_sclr* plan, const kfft_s
     if (!plan->basis || (plan->basis->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
     if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->basis->gpu;
-    EvalGuard guard(g);
     cudaSetDevice(current_device());
     cudaStream_t st = sync_stream();
     const uint32_t bins = real_bins(plan);
@@ -885,7 +938,6 @@ KFFT_API kfft_return_t kfft_evali_scalar_batch(kfft_plan_sclr* plan, const kfft_
     if (!plan->basis || !(plan->basis->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
     if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->basis->gpu;
-    EvalGuard guard(g);
     cudaSetDevice(current_device());
     cudaStream_t st = sync_stream();
     const uint32_t bins = real_bins(plan);
@@ -1047,7 +1099,8 @@ KFFT_API kfft_plan_c2d* kfft_config2_cpx(const uint32_t x_size, const uint32_t y
 
 namespace {
 // 2D complex transform on device buffers (rows of x, y rows)
-bool c2d_dev(const kfft_plan_c2d* p, const vec2_t* din, vec2_t* dout, Carve& cv, cudaStream_t st) {
+bool c2d_dev(const kfft_plan_c2d* p, const vec2_t* din, vec2_t* dout, Carve& cv, cudaStream_t st,
+             const Product& pr = Product()) {
     const FftPlan* Px = gp(p->plan_x);
     const FftPlan* Py = gp(p->plan_y);
     if (!Px || !Py) return false;
@@ -1056,7 +1109,7 @@ bool c2d_dev(const kfft_plan_c2d* p, const vec2_t* din, vec2_t* dout, Carve& cv,
     void* w = cv.take(wb);
     if (wb && !w) return false;
     if (!run_cpx(*Px, din, dout, y, inverse_scale(p->flags, x), w, wb, st)) return false;
-    return run_columns(*Py, dout, x, y, inverse_scale(p->flags, y), cv, st);
+    return run_columns(*Py, dout, x, y, inverse_scale(p->flags, y), cv, st, pr);
 }
 
 size_t c2d_bytes(const kfft_plan_c2d* p) {
@@ -1103,7 +1156,6 @@ KFFT_API kfft_return_t kfft_eval2_cpx(kfft_plan_c2d* cfg, const kfft_cpx* fin, k
     if (!cfg || !fin || !fout) return KFFT_RET_BADARGUMENTS;
     if (cfg->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = cfg->plan_x->gpu;
-    EvalGuard guard(g);
     const size_t bytes = sizeof(vec2_t) * size_t(cfg->nfft);
     const void* ins[1] = {fin};
     return with_staging(g, c2d_bytes(cfg), ins, &bytes, 1, fout, bytes,
@@ -1154,11 +1206,11 @@ KFFT_API kfft_plan_s2d* kfft_config2_scalar(const uint32_t x_size, const uint32_
 namespace {
 // real 2D forward on device: rows real (expanded) -> complex columns
 bool s2d_forward_dev(const kfft_plan_s2d* p, const real_t* din, vec2_t* dout, Carve& cv,
-                     cudaStream_t st) {
+                     cudaStream_t st, const Product& pr = Product()) {
     const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(p->plan_x);
     const kfft_plan_cpx* cy = reinterpret_cast<const kfft_plan_cpx*>(p->plan_y);
     if (!real_forward_dev(rx, din, dout, p->y, p->x, 1, cv, st)) return false;
-    return run_columns(*gp(cy), dout, p->x, p->y, real_t(1), cv, st);
+    return run_columns(*gp(cy), dout, p->x, p->y, real_t(1), cv, st, pr);
 }
 size_t s2d_forward_bytes(const kfft_plan_s2d* p) {
     const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(p->plan_x);
@@ -1206,7 +1258,6 @@ KFFT_API kfft_return_t kfft_eval2_scalar(kfft_plan_s2d* plan, const kfft_scalar*
     if (plan->flags & KFFT_FLAG_INVERSE) return KFFT_RET_IMPROPER_PLAN;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = s2d_handle(plan);
-    EvalGuard guard(g);
     const size_t ib = sizeof(real_t) * size_t(plan->nfft), ob = sizeof(vec2_t) * size_t(plan->nfft);
     const void* ins[1] = {fin};
     return with_staging(g, s2d_forward_bytes(plan), ins, &ib, 1, fout, ob,
@@ -1222,7 +1273,6 @@ KFFT_API kfft_return_t kfft_evali2_scalar(kfft_plan_s2d* plan, const kfft_cpx* f
     if (!(plan->flags & KFFT_FLAG_INVERSE)) return KFFT_RET_IMPROPER_PLAN;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = s2d_handle(plan);
-    EvalGuard guard(g);
     const size_t ib = sizeof(vec2_t) * size_t(plan->nfft), ob = sizeof(real_t) * size_t(plan->nfft);
     const void* ins[1] = {fin};
     return with_staging(g, s2d_inverse_bytes(plan), ins, &ib, 1, fout, ob,
@@ -1258,7 +1308,6 @@ KFFT_API kfft_return_t kfft_eval_conv_cpx(kfft_plan_ccnv* plan, const kfft_cpx* 
     if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->plan_fwd->gpu;
-    EvalGuard guard(g);
     const FftPlan& F = *gp(plan->plan_fwd);
     const FftPlan& I = *gp(plan->plan_inv);
     const uint32_t n = plan->nfft;
@@ -1275,9 +1324,14 @@ KFFT_API kfft_return_t kfft_eval_conv_cpx(kfft_plan_ccnv* plan, const kfft_cpx* 
                             if (!fa || !fb || (wb && !w)) return false;
                             if (!run_cpx(F, static_cast<const vec2_t*>(di[0]), fa, 1, real_t(1), w, wb, st))
                                 return false;
-                            if (!run_cpx(F, static_cast<const vec2_t*>(di[1]), fb, 1, real_t(1), w, wb, st))
+                            // the spectrum product rides on B's last forward pass when it can
+                            bool fused = false;
+                            Product pr;
+                            pr.mul = fa;
+                            pr.fused = &fused;
+                            if (!run_cpx(F, static_cast<const vec2_t*>(di[1]), fb, 1, real_t(1), w, wb, st, pr))
                                 return false;
-                            launch_hadamard(fb, fa, n, st);
+                            if (!fused) launch_hadamard(fb, fa, n, st);
                             return run_cpx(I, fb, static_cast<vec2_t*>(dout), 1,
                                            inverse_scale(plan->plan_inv->flags, n), w, wb, st);
                         });
@@ -1308,7 +1362,6 @@ KFFT_API kfft_return_t kfft_eval_conv_scalar(kfft_plan_scnv* plan, const kfft_sc
     if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->plan_fwd->basis->gpu;
-    EvalGuard guard(g);
     const uint32_t n = plan->nfft;
     const uint32_t bins = real_bins(plan->plan_fwd);
     const size_t rb = sizeof(real_t) * size_t(n);
@@ -1328,11 +1381,15 @@ KFFT_API kfft_return_t kfft_eval_conv_scalar(kfft_plan_scnv* plan, const kfft_sc
                                                   fa, 1, bins, ex, cv, st))
                                 return false;
                             cv.used = mark;
+                            bool fused = false;
+                            Product pr;
+                            pr.mul = fa;
+                            pr.fused = &fused;
                             if (!real_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[1]),
-                                                  fb, 1, bins, ex, cv, st))
+                                                  fb, 1, bins, ex, cv, st, pr))
                                 return false;
                             cv.used = mark;
-                            launch_hadamard(fb, fa, bins, st);
+                            if (!fused) launch_hadamard(fb, fa, bins, st);
                             return real_inverse_dev(plan->plan_inv, fb, bins,
                                                     static_cast<real_t*>(dout), 1, cv, st);
                         });
@@ -1368,7 +1425,6 @@ KFFT_API kfft_return_t kfft_eval2_conv_cpx(kfft_plan_c2cnv* plan, const kfft_cpx
     if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = plan->plan_fwd->plan_x->gpu;
-    EvalGuard guard(g);
     const size_t bytes = sizeof(vec2_t) * size_t(plan->nfft);
     const size_t work = 2 * r256(bytes) + std::max(c2d_bytes(plan->plan_fwd), c2d_bytes(plan->plan_inv));
     const void* ins[2] = {fin_A, fin_B};
@@ -1382,10 +1438,14 @@ KFFT_API kfft_return_t kfft_eval2_conv_cpx(kfft_plan_c2cnv* plan, const kfft_cpx
                             if (!c2d_dev(plan->plan_fwd, static_cast<const vec2_t*>(di[0]), fa, cv, st))
                                 return false;
                             cv.used = mark;
-                            if (!c2d_dev(plan->plan_fwd, static_cast<const vec2_t*>(di[1]), fb, cv, st))
+                            bool fused = false;
+                            Product pr;
+                            pr.mul = fa;
+                            pr.fused = &fused;
+                            if (!c2d_dev(plan->plan_fwd, static_cast<const vec2_t*>(di[1]), fb, cv, st, pr))
                                 return false;
                             cv.used = mark;
-                            launch_hadamard(fb, fa, plan->nfft, st);
+                            if (!fused) launch_hadamard(fb, fa, plan->nfft, st);
                             return c2d_dev(plan->plan_inv, fb, static_cast<vec2_t*>(dout), cv, st);
                         });
 }
@@ -1419,7 +1479,6 @@ KFFT_API kfft_return_t kfft_eval2_conv_scalar(kfft_plan_s2cnv* plan, const kfft_
     if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = s2d_handle(plan->plan_fwd);
-    EvalGuard guard(g);
     const size_t n = plan->nfft;
     const size_t rb = sizeof(real_t) * n, sb = sizeof(vec2_t) * n;
     const size_t work = 2 * r256(sb) + std::max(s2d_forward_bytes(plan->plan_fwd),
@@ -1435,10 +1494,14 @@ KFFT_API kfft_return_t kfft_eval2_conv_scalar(kfft_plan_s2cnv* plan, const kfft_
                             if (!s2d_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[0]), fa, cv, st))
                                 return false;
                             cv.used = mark;
-                            if (!s2d_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[1]), fb, cv, st))
+                            bool fused = false;
+                            Product pr;
+                            pr.mul = fa;
+                            pr.fused = &fused;
+                            if (!s2d_forward_dev(plan->plan_fwd, static_cast<const real_t*>(di[1]), fb, cv, st, pr))
                                 return false;
                             cv.used = mark;
-                            launch_hadamard(fb, fa, n, st);
+                            if (!fused) launch_hadamard(fb, fa, n, st);
                             return s2d_inverse_dev(plan->plan_inv, fb, static_cast<real_t*>(dout), cv, st);
                         });
 }

@@ -68,6 +68,27 @@ enum : uint8_t {
     EPI_CHIRP = 2,     // k < bound: out[b*bs + k*es] = v * tab[k] * scale
     EPI_RADER_FWD = 3, // out[..k..] = v * tab[k]; k == 0: aux_out[2b] = x0, aux_out[2b+1] = x0 + v
     EPI_RADER_INV = 4, // aux_out[b*bs + perm[k]*es] = (v + x0) * scale; k == 0 also X_0
+    EPI_MUL_OUT = 5,   // out[i] = v * tab[i] * scale, i = b*bs + k*es: a table in the output's
+                       // layout (the other operand's spectrum of a convolution)
+};
+
+// Where a fused convolution pass (PassDesc::fuse) stores its result: the
+// first pass of the inverse transform, whose lanes are the forward last
+// pass's lanes (element j*R + r of sequence b), with that pass's epilogue
+// (EPI_NONE, EPI_CHIRP or EPI_RADER_INV when the inverse has one pass only).
+struct FuseTail {
+    vec2_t* out;
+    uint64_t out_bs;
+    uint32_t out_es;
+    uint8_t epi_op;
+    const vec2_t* epi_tab;
+    const uint32_t* epi_perm;
+    uint32_t epi_bound;
+    const vec2_t* aux_in;
+    vec2_t* aux_out;
+    uint64_t aux_out_bs;
+    uint32_t aux_out_es;
+    real_t scale;
 };
 
 struct PassDesc {
@@ -111,6 +132,14 @@ struct PassDesc {
     uint64_t aux_in_bs, aux_out_bs;
     uint32_t aux_out_es;
     real_t scale;
+    // Fused convolution pass: after its R-point DFTs (the last pass of a
+    // forward transform) each value is multiplied by the epilogue's spectrum
+    // (EPI_MUL or EPI_RADER_FWD) and conjugated in shared memory, the same
+    // inner stages run again (an R-point forward DFT of the conjugate is the
+    // conjugate of the inverse DFT) and the conjugated result goes to `tail`:
+    // the first pass of the inverse transform, one HBM round trip saved.
+    uint8_t fuse;
+    FuseTail tail;
 };
 
 // ---- device tables -----------------------------------------------------
@@ -147,8 +176,11 @@ bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t*
                        uint32_t max_polls = kQueueMaxPolls);
 // Even-N real transform post-processing (kfft_scalar.c:174-216): z holds the
 // N/2-point spectrum of each sequence, out gets nbins bins per sequence.
+// With `mul` (a spectrum in the output's layout) every bin written is also
+// multiplied by mul's bin: the product of a convolution, fused into the store.
 void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32_t h,
-                      uint32_t batch, uint64_t out_bs, int expand, cudaStream_t st);
+                      uint32_t batch, uint64_t out_bs, int expand, cudaStream_t st,
+                      const vec2_t* mul = nullptr);
 // Even-N real inverse pre-processing (kfft_scalar.c:218-242).
 void launch_real_pre(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
                      uint32_t batch, uint64_t in_bs, cudaStream_t st);
@@ -252,8 +284,11 @@ std::string describe(const FftPlan& p);
 // Device workspace (bytes) the plan needs for `batch` sequences.
 size_t workspace_bytes(const FftPlan& p, uint32_t batch);
 // Appends the passes computing out = FFT(in) * scale to `descs`.
+// With `fuse`, the forward last pass and the inverse first pass of a Rader
+// or Bluestein convolution become one fused pass where they can.
 bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t* out,
-                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
+                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs,
+                  bool fuse = true);
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
 // Descriptor of pass `pass` of a DIRECT plan (no fused element operations).
 // Start of chunk i (i = 0..k; chunk k's start is `total`) when `total` units
@@ -305,6 +340,18 @@ PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const L
 const FftPlan* device_plan_of(const kfft_plan_cpx* p);
 
 // ---- runtime ----------------------------------------------------------------
+// Bounded device waits that can run out (the bulk-copy waits of k_pass_bulk)
+// record the failure in a per-host-thread slot of a device array.
+constexpr int kWaitSlots = 64;
+// Polls of a bulk-copy wait before it gives up (about a second of try_wait
+// suspensions); a test hook can lower it.
+constexpr uint32_t kBulkMaxPolls = 1u << 22;
+int wait_slot();
+// After the work queued on `st` is done: reads and clears this thread's slot;
+// true when a wait ran out since the last check.
+bool take_wait_failures(cudaStream_t st);
+// Records an engine failure that is not a CUDA error (for kfft_gb300_last_error).
+void note_engine_error(const char* msg);
 int current_device();
 bool ensure_device();
 void note_cuda_error(cudaError_t e);

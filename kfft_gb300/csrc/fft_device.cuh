@@ -15,6 +15,7 @@
 #include <cuda_fp16.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "engine.cuh"
 
@@ -286,11 +287,103 @@ __device__ __forceinline__ void dft_odd(vec2_t* v) {
 }
 
 template <int P, bool INV>
+__device__ __forceinline__ void dft(vec2_t* v);
+
+// ---------------------------------------------------------------------------
+// composite radices 6, 9, 10, 12, 14, 15: a P = A*B point DFT in registers
+// from A-point and B-point butterflies, so a mixed-radix tile runs fewer
+// inner stages (each stage is a shared-memory round trip and a barrier).
+// Coprime A, B use the Good-Thomas map (input n = (B n1 + A n2) mod P,
+// output k = (B (B^-1 mod A) k1 + A (A^-1 mod B) k2) mod P, no twiddles);
+// 9 = 3*3 uses Cooley-Tukey (n = 3 n1 + n2, k = k1 + 3 k2) with the
+// twiddles W_9^(n2 k1) as instruction immediates.  Every index is a
+// template constant, so the values stay in registers.
+// ---------------------------------------------------------------------------
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+constexpr int cgcd(int a, int b) { return b == 0 ? a : cgcd(b, a % b); }
+// inverse of a modulo m (gcd(a, m) = 1)
+constexpr int cinv(int a, int m) {
+    for (int x = 1; x < m; ++x)
+        if ((a * x) % m == 1) return x;
+    return 1 % m;
+}
+
+// a * W_P^E (forward W = exp(-2 pi i / P)), E taken modulo P; quarter turns
+// are exact rotations
+template <int P, int E, bool INV>
+__device__ __forceinline__ vec2_t wmul_const(vec2_t a) {
+    constexpr int e = ((E % P) + P) % P;
+    if constexpr (e == 0) {
+        return a;
+    } else if constexpr ((4 * e) % P == 0) {
+        constexpr int q = (4 * e) / P;  // quarter turns, 1..3
+        if constexpr (q == 2) return vec2_t{-a.x, -a.y};
+        else if constexpr (q == 1) return rot<INV>(a);
+        else return rot<!INV>(a);
+    } else {
+        constexpr real_t c = real_t(trig_ratio(e, P, false));
+        constexpr real_t s = real_t(trig_ratio(e, P, true));
+        constexpr real_t wi = INV ? s : -s;  // W^e = cos - i sin (forward)
+        return {a.x * c - a.y * wi, a.x * wi + a.y * c};
+    }
+}
+
+template <int A, int B, bool INV>
+__device__ __forceinline__ void dft_composite(vec2_t* v) {
+    constexpr int P = A * B;
+    constexpr bool kPfa = cgcd(A, B) == 1;
+    vec2_t t[P];  // t[n2 * A + k1]
+    static_for<0, B>([&](auto n2c) {
+        constexpr int n2 = decltype(n2c)::value;
+        vec2_t a[A];
+        static_for<0, A>([&](auto n1c) {
+            constexpr int n1 = decltype(n1c)::value;
+            constexpr int n = kPfa ? (B * n1 + A * n2) % P : B * n1 + n2;
+            a[n1] = v[n];
+        });
+        dft<A, INV>(a);
+        static_for<0, A>([&](auto k1c) {
+            constexpr int k1 = decltype(k1c)::value;
+            if constexpr (kPfa) t[n2 * A + k1] = a[k1];
+            else t[n2 * A + k1] = wmul_const<P, n2 * k1, INV>(a[k1]);
+        });
+    });
+    static_for<0, A>([&](auto k1c) {
+        constexpr int k1 = decltype(k1c)::value;
+        vec2_t b[B];
+        static_for<0, B>([&](auto n2c) {
+            constexpr int n2 = decltype(n2c)::value;
+            b[n2] = t[n2 * A + k1];
+        });
+        dft<B, INV>(b);
+        static_for<0, B>([&](auto k2c) {
+            constexpr int k2 = decltype(k2c)::value;
+            constexpr int k = kPfa ? (B * cinv(B % A, A) * k1 + A * cinv(A % B, B) * k2) % P
+                                   : k1 + A * k2;
+            v[k] = b[k2];
+        });
+    });
+}
+
+template <int P, bool INV>
 __device__ __forceinline__ void dft(vec2_t* v) {
     if constexpr (P == 2) dft2<INV>(v[0], v[1]);
     else if constexpr (P == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
     else if constexpr (P == 8) dft8<INV>(v);
     else if constexpr (P == 16) dft16<INV>(v);
+    else if constexpr (P == 6) dft_composite<2, 3, INV>(v);
+    else if constexpr (P == 9) dft_composite<3, 3, INV>(v);
+    else if constexpr (P == 10) dft_composite<2, 5, INV>(v);
+    else if constexpr (P == 12) dft_composite<4, 3, INV>(v);
+    else if constexpr (P == 14) dft_composite<2, 7, INV>(v);
+    else if constexpr (P == 15) dft_composite<3, 5, INV>(v);
     else dft_odd<P, INV>(v);
 }
 
@@ -347,9 +440,15 @@ __device__ __forceinline__ void run_inner(int P, const vec2_t* src, vec2_t* dst,
         case 4: inner_pass<4, INV>(src, dst, R, C, st, tw); break;
         case 5: inner_pass<5, INV>(src, dst, R, C, st, tw); break;
         case 7: inner_pass<7, INV>(src, dst, R, C, st, tw); break;
+        case 6: inner_pass<6, INV>(src, dst, R, C, st, tw); break;
         case 8: inner_pass<8, INV>(src, dst, R, C, st, tw); break;
+        case 9: inner_pass<9, INV>(src, dst, R, C, st, tw); break;
+        case 10: inner_pass<10, INV>(src, dst, R, C, st, tw); break;
         case 11: inner_pass<11, INV>(src, dst, R, C, st, tw); break;
+        case 12: inner_pass<12, INV>(src, dst, R, C, st, tw); break;
         case 13: inner_pass<13, INV>(src, dst, R, C, st, tw); break;
+        case 14: inner_pass<14, INV>(src, dst, R, C, st, tw); break;
+        case 15: inner_pass<15, INV>(src, dst, R, C, st, tw); break;
         case 16: inner_pass<16, INV>(src, dst, R, C, st, tw); break;
         default: break;
     }
@@ -388,6 +487,11 @@ __device__ __forceinline__ void store_elem(const PassDesc& d, uint32_t b, uint32
                 d.aux_out[2 * uint64_t(b) + 1] = cadd(x0, v);
             }
             break;
+        case EPI_MUL_OUT: {
+            const uint64_t i = b * d.out_bs + uint64_t(k) * d.out_es;
+            d.out[i] = cscale(cmul(v, __ldcg(&d.epi_tab[i])), d.scale);
+            break;
+        }
         case EPI_RADER_INV: {
             // X[g^-k] = x_0 + c_k, and X_0 from the saved pair; never reads the input,
             // so the transform may run in place
@@ -517,7 +621,12 @@ __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x,
 // (with the epilogue), and only the exchanges between inner passes go through
 // one shared-memory buffer (read all, barrier, write all, barrier).
 // ---------------------------------------------------------------------------
-enum : int { IO_SMEM = 0, IO_GLOBAL = 1 };
+// Where a stage of the register tile reads or writes: shared memory, global
+// memory (the pass's prologue / epilogue), or, in a fused convolution pass,
+// shared memory through the spectrum product and a conjugation (IO_MID, the
+// forward half's last stage) and global memory through the tail store with a
+// conjugation (IO_TAIL, the inverse half's last stage).
+enum : int { IO_SMEM = 0, IO_GLOBAL = 1, IO_MID = 2, IO_TAIL = 3 };
 
 // v[q] *= W^(q*step) for q = 1..P-1, W^i = tw[i].  FP64 loads every factor
 // (the FP64 pipe, not the loads, bounds it).  FP32 loads the four anchors
@@ -550,6 +659,44 @@ __device__ __forceinline__ void apply_inner_twiddles(vec2_t* v, const vec2_t* __
 #endif
 #pragma unroll
     for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&tw[q * step]));
+}
+
+__device__ __forceinline__ vec2_t conj2(vec2_t a) { return {a.x, -a.y}; }
+
+// Spectrum product of a fused convolution pass at forward output index k of
+// sequence b (EPI_MUL, or EPI_RADER_FWD with its bin-0 bookkeeping), returned
+// conjugated for the inverse half.
+__device__ __forceinline__ vec2_t fuse_mid(const PassDesc& d, uint32_t b, uint32_t k, vec2_t v) {
+    if (d.epi_op == EPI_RADER_FWD && k == 0) {
+        const vec2_t x0 = __ldcg(&d.aux_in[b * d.aux_in_bs]);
+        d.aux_out[2 * uint64_t(b)] = x0;
+        d.aux_out[2 * uint64_t(b) + 1] = cadd(x0, v);
+    }
+    return conj2(cmul(v, __ldg(&d.epi_tab[k])));
+}
+
+// Store of a fused convolution pass: element k of sequence b of the inverse
+// transform's first pass, after undoing the conjugation, through that pass's
+// epilogue (the cases an inverse first pass can carry).
+__device__ __forceinline__ void store_tail(const FuseTail& t, uint32_t b, uint32_t k, vec2_t v) {
+    v = conj2(v);
+    switch (t.epi_op) {
+        case EPI_CHIRP:
+            if (k < t.epi_bound)
+                t.out[b * t.out_bs + uint64_t(k) * t.out_es] = cscale(cmul(v, __ldg(&t.epi_tab[k])), t.scale);
+            break;
+        case EPI_RADER_INV: {
+            const vec2_t x0 = __ldcg(&t.aux_in[2 * uint64_t(b)]);
+            const uint32_t idx = __ldg(&t.epi_perm[k]);
+            vec2_t* o = t.aux_out + b * t.aux_out_bs;
+            o[uint64_t(idx) * t.aux_out_es] = cscale(cadd(v, x0), t.scale);
+            if (k == 0) o[0] = cscale(__ldcg(&t.aux_in[2 * uint64_t(b) + 1]), t.scale);
+            break;
+        }
+        default:
+            t.out[b * t.out_bs + uint64_t(k) * t.out_es] = cscale(v, t.scale);
+            break;
+    }
 }
 
 // The P inputs of one butterfly of the first inner pass, straight from global
@@ -666,7 +813,7 @@ __device__ __forceinline__ void fused_store(const PassDesc& d, uint32_t bs, uint
 // butterfly at a time from `src` (global memory on the first pass, else a
 // shared buffer) and writes it to `dst` (global memory on the last pass, else
 // the other shared buffer).
-template <int P, bool INV>
+template <int P, bool INV, bool FUSE>
 __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& st,
                                            const vec2_t* src, vec2_t* dst, uint32_t lane0,
                                            uint32_t total, int sio, int dio) {
@@ -674,6 +821,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
     const uint32_t items = d.C * m;
     const bool cfast = (sio == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
                                           : ((dio == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
+    const bool need_lane = sio == IO_GLOBAL || dio != IO_SMEM;
     for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
         uint32_t c, jj;
         if (cfast) {
@@ -686,7 +834,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         const uint32_t g = lane0 + c;
         uint32_t bs = 0, j = 0;
         const bool live = g < total;
-        if ((sio == IO_GLOBAL || dio == IO_GLOBAL) && live) {
+        if (need_lane && live) {
             if (d.order == ORDER_J) {
                 bs = fdiv(g, d.div_lanes_j);
                 j = g - bs * d.lanes_j;
@@ -715,8 +863,22 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         if (dio == IO_SMEM) {
 #pragma unroll
             for (int q = 0; q < P; ++q) dst[c * d.lane_stride + pad(ob + q * st.ns)] = v[q];
+        } else if (FUSE && dio == IO_MID) {
+            // forward output index k = j + r Ns of the last pass (blo = 0)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const uint32_t r = ob + q * st.ns;
+                dst[c * d.lane_stride + pad(r)] =
+                    live ? fuse_mid(d, bs, j + r * d.Ns, v[q]) : vec2_t{real_t(0), real_t(0)};
+            }
         } else if (live) {
-            fused_store<P>(d, bs, j, ob, st.ns, v);
+            if (FUSE && dio == IO_TAIL) {
+                // the inverse's first pass: lane j holds elements j R + r
+#pragma unroll
+                for (int q = 0; q < P; ++q) store_tail(d.tail, bs, j * d.R + ob + q * st.ns, v[q]);
+            } else {
+                fused_store<P>(d, bs, j, ob, st.ns, v);
+            }
         }
     }
 }
@@ -1135,10 +1297,11 @@ __device__ __forceinline__ void tile_loop_pipelined(const PassDesc& d, vec2_t* s
 
 #if defined(KFFT_HALF_SCALAR)
 // ---------------------------------------------------------------------------
-// single-pass power-of-two tiles fed by the tensor memory accelerator: the
-// C sequences of a tile are C*R contiguous points, so one bulk copy
-// (cp.async.bulk, completion counted on an mbarrier) moves the next tile
-// into shared memory while the current one's later stages run.
+// single-pass power-of-two tiles fed by one-dimensional bulk copies: the C
+// sequences of a tile are C*R contiguous points, so one untiled bulk copy
+// (cp.async.bulk global -> shared, no tensor map; completion counted on an
+// mbarrier) moves the next tile into shared memory while the current one's
+// later stages run.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return uint32_t(__cvta_generic_to_shared(p));
@@ -1160,26 +1323,39 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
-// bounded wait for phase `parity` of `bar`; false when the limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
+// Bounded wait for phase `parity` of `bar`; false when `max_polls` polls ran
+// out.  The first poll is a non-blocking test_wait (the copy has usually
+// landed long before its tile's turn), the others are try_wait, which may
+// suspend the thread for a hardware-defined time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
+    for (uint32_t it = 0; it < max_polls; ++it) {
         uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n"
-            " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (it == 0) {
+            asm volatile(
+                "{\n .reg .pred p;\n"
+                " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                " selp.u32 %0, 1, 0, p;\n}"
+                : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        } else {
+            asm volatile(
+                "{\n .reg .pred p;\n"
+                " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                " selp.u32 %0, 1, 0, p;\n}"
+                : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        }
         if (done) return true;
     }
     return false;
 }
 
 // Shared memory: [mbarrier | pad to 128 B | raw tile C*R | bufA | bufB].
-// A wait that runs out (only a failed copy can cause it) ends the CTA after
-// recording the failure in *fail.
+// A wait that runs out after `max_polls` polls (only a failed or very slow
+// copy can cause it) sets *fail; the CTA then waits once more, with the
+// default limit, for the copy in flight to land and ends without finishing
+// its tiles, so the caller must treat the output as invalid.
 template <uint32_t R, bool INV>
 __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char* smem,
-                                               uint32_t* fail) {
+                                               uint32_t* fail, uint32_t max_polls) {
     constexpr uint32_t L = ilog2(R);
     constexpr uint32_t K16 = L / 4;
     constexpr int T = 1 << (L % 4);
@@ -1212,10 +1388,10 @@ __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char*
         // every thread waits (the mbarrier's completion makes the copied data
         // visible to it); the CTA leaves together if any wait ran out, after
         // a second bounded wait that lets the copy in flight land first
-        const bool ok = mbar_wait(bar, parity);
+        const bool ok = mbar_wait(bar, parity, max_polls);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) atomicExch(fail, 1u);
-            mbar_wait(bar, parity);
+            mbar_wait(bar, parity, kBulkMaxPolls);
             return;
         }
         parity ^= 1u;
@@ -1263,20 +1439,26 @@ __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char*
 }
 #endif
 
-template <bool INV>
+template <bool INV, bool FUSE>
 __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
                                                const vec2_t* src, vec2_t* dst, uint32_t lane0,
                                                uint32_t total, int sio, int dio) {
     switch (P) {
-        case 2: fused_pass<2, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 3: fused_pass<3, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 4: fused_pass<4, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 5: fused_pass<5, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 7: fused_pass<7, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 8: fused_pass<8, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 11: fused_pass<11, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 13: fused_pass<13, INV>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 16: fused_pass<16, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 2: fused_pass<2, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 3: fused_pass<3, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 4: fused_pass<4, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 5: fused_pass<5, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 7: fused_pass<7, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 6: fused_pass<6, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 8: fused_pass<8, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 9: fused_pass<9, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 10: fused_pass<10, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 11: fused_pass<11, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 12: fused_pass<12, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 13: fused_pass<13, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 14: fused_pass<14, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 15: fused_pass<15, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 16: fused_pass<16, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
         default: break;
     }
 }
@@ -1289,7 +1471,9 @@ __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const I
 // the pass kernel launches those as kernels of their own and leaves it off.
 // TC: keep the tensor-core radix-16 stage; the queue kernel leaves it off
 // (its planner clears d.tc) to keep its instruction footprint small.
-template <bool INV, bool SPEC = true, bool TC = true>
+// FUSE: run fused convolution passes (PassDesc::fuse); the queue kernel
+// leaves it off (its planner does not fuse) to keep its body small.
+template <bool INV, bool SPEC = true, bool TC = true, bool FUSE = true>
 __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra& x, uint32_t tile,
                                               vec2_t* sm) {
     const uint32_t total = d.batch * d.lanes_j;
@@ -1336,16 +1520,22 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
         Gm = dft16_frag<INV>(2);
     }
 #endif
-    for (int p = 0; p < np; ++p) {
-        const bool last = (p + 1 == np);
-        vec2_t* dst = last ? nullptr : ((p % 2 == 0) ? bufA : bufB);
-        const int sio = p == 0 ? IO_GLOBAL : IO_SMEM, dio = last ? IO_GLOBAL : IO_SMEM;
+    // a fused convolution pass runs the inner stages twice: the forward
+    // half ends in shared memory (IO_MID), the inverse half in the tail store
+    const bool fuse = FUSE && d.fuse;
+    const int ns_total = fuse ? 2 * np : np;
+    for (int s = 0; s < ns_total; ++s) {
+        const int p = s < np ? s : s - np;
+        const bool last = (s + 1 == ns_total);
+        vec2_t* dst = last ? nullptr : ((s % 2 == 0) ? bufA : bufB);
+        const int sio = s == 0 ? IO_GLOBAL : IO_SMEM;
+        const int dio = last ? (fuse ? IO_TAIL : IO_GLOBAL) : (fuse && s == np - 1 ? IO_MID : IO_SMEM);
 #if defined(KFFT_HALF_SCALAR)
         if (TC && d.tc && d.rad[p] == 16)
             tc_pass16<INV>(d, x.step[p], src, dst, lane0, total, sio, dio, Fr, Fi, Gm);
         else
 #endif
-            fused_dispatch<INV>(d.rad[p], d, x.step[p], src, dst, lane0, total, sio, dio);
+            fused_dispatch<INV, FUSE>(d.rad[p], d, x.step[p], src, dst, lane0, total, sio, dio);
         if (!last) __syncthreads();
         src = dst;
     }

@@ -13,7 +13,11 @@
 // The array holds kNoAllocScratchBytes (32 MiB) on every GPU that loads this
 // library, for the life of the process.  Its device address is looked up once
 // per device, on the first call made with that device current; that first call
-// should come before any stream capture.  All calls share the array and it
+// should come before any stream capture.  The first call with a given plan and
+// batch may also do one-time set-up of the pass kernels it picks (their
+// shared-memory limit and occupancy query, and the lazy load of their module),
+// so run every (plan, batch) shape once before a region that must not do
+// that.  All calls share the array and it
 // keeps the last call's contents; nothing in it has to start at zero, because
 // every pass writes its whole output before the next pass reads it.  Calls
 // whose kernels overlap on the GPU (different streams, or different host
@@ -38,7 +42,8 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_setup_mu;
 void* g_scratch_addr[kMaxDevices] = {};
-char g_noalloc_msg[256] = "";
+// why this thread's last call was rejected ("" after a call that was not)
+thread_local char g_noalloc_msg[256] = "";
 
 // Device address of the scratch array on the current device (set-up on first use).
 void* scratch_address(int dev) {
@@ -76,6 +81,7 @@ KFFT_API const char* kfft_noalloc_last_message(void) { return g_noalloc_msg; }
 
 KFFT_API kfft_return_t kfft_eval_cpx_noalloc(kfft_plan_cpx* plan, const kfft_cpx* fin,
                                              kfft_cpx* fout, uint32_t batch, void* stream) {
+    g_noalloc_msg[0] = '\0';
     if (!plan || !fin || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0 || batch == 0) return KFFT_RET_SUCCESS;
     const FftPlan* fp = device_plan_of(plan);

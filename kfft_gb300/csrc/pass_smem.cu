@@ -14,20 +14,27 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(const __grid_constant__ P
     tile_body<INV, BIG>(d, x, blockIdx.x, reinterpret_cast<vec2_t*>(smem_raw));
 }
 
+// One-time shared-memory limit of the shared-memory tile kernels; the
+// initialisation of a function-local static is thread-safe, and a failure is
+// reported on every call.
 static bool configure_pass_kernels() {
-    static bool done = false;
-    if (done) return true;
-    const void* fns[4] = {(const void*)k_pass<false, false>, (const void*)k_pass<true, false>,
-                          (const void*)k_pass<false, true>, (const void*)k_pass<true, true>};
-    for (const void* f : fns) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        if (e != cudaSuccess) {
-            note_cuda_error(e);
-            return false;
+    static const cudaError_t status = [] {
+        const void* fns[4] = {(const void*)k_pass<false, false>, (const void*)k_pass<true, false>,
+                              (const void*)k_pass<false, true>, (const void*)k_pass<true, true>};
+        for (const void* f : fns) {
+            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 227 * 1024);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return e;
+            }
         }
+        return cudaSuccess;
+    }();
+    if (status != cudaSuccess) {
+        note_cuda_error(status);
+        return false;
     }
-    done = true;
     return true;
 }
 

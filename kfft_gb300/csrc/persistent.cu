@@ -3,6 +3,8 @@
 // on per-pass tile counters (a wait that gives up sets an error word).
 #include "fft_device.cuh"
 
+#include <mutex>
+
 namespace kfft {
 
 __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent(
@@ -44,8 +46,8 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
         __syncthreads();
         if (s_ok) {
             const PassExtra& x = extras[q.desc];
-            if (s_desc.inv) tile_body_reg<true, true, false>(s_desc, x, q.tile, buf);
-            else tile_body_reg<false, true, false>(s_desc, x, q.tile, buf);
+            if (s_desc.inv) tile_body_reg<true, true, false, false>(s_desc, x, q.tile, buf);
+            else tile_body_reg<false, true, false, false>(s_desc, x, q.tile, buf);
         }
         __threadfence();
         __syncthreads();
@@ -57,28 +59,35 @@ bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t*
                        const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
                        uint32_t* error, uint32_t smem_bytes, cudaStream_t st,
                        uint32_t max_polls) {
+    // the kernel's shared-memory limit and occupancy, set up under a lock (several
+    // host threads may record queues at once)
+    static std::mutex mu;
     static int blocks_per_sm = -1;
     static uint32_t configured_smem = 0;
     static int sms = 0;
-    if (configured_smem < smem_bytes) {
-        cudaError_t e = cudaFuncSetAttribute(k_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(smem_bytes));
-        if (e != cudaSuccess) {
-            note_cuda_error(e);
-            return false;
+    uint32_t grid;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (configured_smem < smem_bytes) {
+            cudaError_t e = cudaFuncSetAttribute(
+                k_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
+            if (e != cudaSuccess) {
+                note_cuda_error(e);
+                return false;
+            }
+            configured_smem = smem_bytes;
+            blocks_per_sm = -1;
         }
-        configured_smem = smem_bytes;
-        blocks_per_sm = -1;
+        if (blocks_per_sm < 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_persistent,
+                                                          kPassThreads, configured_smem);
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+        grid = uint32_t(sms * blocks_per_sm);
     }
-    if (blocks_per_sm < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_persistent, kPassThreads,
-                                                      smem_bytes);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
-    uint32_t grid = uint32_t(sms * blocks_per_sm);
     if (grid > nitems) grid = nitems ? nitems : 1;
     k_persistent<<<grid, kPassThreads, smem_bytes, st>>>(
         descs, static_cast<const PassExtra*>(extras), deps, static_cast<const QueueItem*>(items),

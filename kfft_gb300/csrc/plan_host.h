@@ -25,22 +25,99 @@ inline std::vector<uint32_t> prime_factors(uint32_t n) {
     return f;
 }
 
-// inner radix schedule of a tile length R: 16s first, then 8/4/2, then odd primes
+// Estimated real flops per point of one inner stage of radix r: the
+// butterfly (register DFT) plus the r-1 twiddle products of a later stage.
+// Used only to break ties between schedules with equally many stages.
+inline double radix_flops_per_point(uint32_t r) {
+    double bfly;
+    switch (r) {
+        case 2: bfly = 4; break;
+        case 3: bfly = 16; break;
+        case 4: bfly = 16; break;
+        case 5: bfly = 40; break;
+        case 6: bfly = 44; break;    // Good-Thomas 2 x 3
+        case 7: bfly = 72; break;
+        case 8: bfly = 52; break;
+        case 9: bfly = 120; break;   // Cooley-Tukey 3 x 3
+        case 10: bfly = 100; break;  // Good-Thomas 2 x 5
+        case 11: bfly = 140; break;
+        case 12: bfly = 112; break;  // Good-Thomas 4 x 3
+        case 13: bfly = 190; break;
+        case 14: bfly = 172; break;  // Good-Thomas 2 x 7
+        case 15: bfly = 200; break;  // Good-Thomas 3 x 5
+        case 16: bfly = 144; break;
+        default: bfly = 4.0 * r * r; break;  // odd primes 17..31
+    }
+    return (bfly + 6.0 * (r - 1)) / r;
+}
+
+// Inner radix schedule of a tile length R.  Powers of two: 16s, then 8, 4 or
+// 2 (the compile-time tile bodies assume exactly this).  Other lengths: the
+// fewest stages whose radices multiply to R, each radix one the register
+// butterflies implement (2-16, including the composites 6, 9, 10, 12, 14,
+// 15), ties broken by the least estimated arithmetic; prime factors 17-31
+// (shared-memory tiles only) are stages of their own.  Every stage is a
+// shared-memory round trip and a barrier, which is what bounds a mixed-radix
+// tile: 729 = 3^6 runs as 9, 9, 9 instead of six radix-3 stages.  Radices are
+// listed largest first.
 inline std::vector<uint8_t> inner_radices(uint32_t R) {
     std::vector<uint8_t> r;
-    uint32_t e2 = 0;
-    while (R % 2 == 0) {
-        R /= 2;
-        ++e2;
+    if (R >= 2 && (R & (R - 1)) == 0) {
+        uint32_t e2 = 0;
+        while ((1u << e2) < R) ++e2;
+        while (e2 >= 4) {
+            r.push_back(16);
+            e2 -= 4;
+        }
+        if (e2 == 3) r.push_back(8);
+        if (e2 == 2) r.push_back(4);
+        if (e2 == 1) r.push_back(2);
+        return r;
     }
-    while (e2 >= 4) {
-        r.push_back(16);
-        e2 -= 4;
+    std::vector<uint8_t> big;
+    uint32_t rest = R;
+    for (uint32_t p : prime_factors(R))
+        if (p > 16) {
+            big.push_back(uint8_t(p));
+            rest /= p;
+        }
+    // best[d]: (stages, flops) of the best schedule of divisor d of `rest`
+    static const uint32_t kSet[] = {16, 15, 14, 13, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+    std::vector<uint32_t> divs;
+    for (uint32_t d = 1; uint64_t(d) * d <= rest; ++d)
+        if (rest % d == 0) {
+            divs.push_back(d);
+            if (d != rest / d) divs.push_back(rest / d);
+        }
+    std::sort(divs.begin(), divs.end());
+    std::vector<uint32_t> stages(divs.size(), 0), pick(divs.size(), 0);
+    std::vector<double> flops(divs.size(), 0.0);
+    auto index_of = [&](uint32_t d) {
+        return size_t(std::lower_bound(divs.begin(), divs.end(), d) - divs.begin());
+    };
+    for (size_t i = 1; i < divs.size(); ++i) {
+        const uint32_t d = divs[i];
+        stages[i] = UINT32_MAX;
+        for (uint32_t q : kSet) {
+            if (d % q) continue;
+            const size_t j = index_of(d / q);
+            if (stages[j] == UINT32_MAX) continue;
+            const uint32_t s = stages[j] + 1;
+            const double f = flops[j] + radix_flops_per_point(q);
+            if (s < stages[i] || (s == stages[i] && f < flops[i] - 1e-9)) {
+                stages[i] = s;
+                flops[i] = f;
+                pick[i] = q;
+            }
+        }
     }
-    if (e2 == 3) r.push_back(8);
-    if (e2 == 2) r.push_back(4);
-    if (e2 == 1) r.push_back(2);
-    for (uint32_t p : prime_factors(R)) r.push_back(uint8_t(p));
+    for (uint32_t d = rest; d > 1;) {
+        const uint32_t q = pick[index_of(d)];
+        r.push_back(uint8_t(q));
+        d /= q;
+    }
+    std::sort(r.rbegin(), r.rend());
+    for (uint8_t p : big) r.push_back(p);
     return r;
 }
 

@@ -142,9 +142,12 @@ void scale_table(vec2_t* t, uint32_t count, double s, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // real transform post/pre processing (kfft_scalar.c:174-242)
 // ---------------------------------------------------------------------------
+// The bins of the even-N real forward transform from the N/2-point spectrum
+// z (kfft_scalar.c:174-216); with `mul`, each stored bin is multiplied by the
+// same bin of mul (a convolution's other spectrum, same layout as out).
 __global__ void k_real_post(const vec2_t* __restrict__ z, vec2_t* __restrict__ out,
                             const vec2_t* __restrict__ stt, uint32_t h, uint32_t batch,
-                            uint64_t out_bs, int expand) {
+                            uint64_t out_bs, int expand, const vec2_t* __restrict__ mul) {
     const uint32_t half = h / 2;  // k = 1..half
     const uint64_t per = uint64_t(half) + 1;
     const uint64_t total = per * batch;
@@ -154,12 +157,14 @@ __global__ void k_real_post(const vec2_t* __restrict__ z, vec2_t* __restrict__ o
         const uint32_t k = uint32_t(t - uint64_t(b) * per);
         const vec2_t* Z = z + uint64_t(b) * h;
         vec2_t* O = out + uint64_t(b) * out_bs;
+        const vec2_t* M = mul ? mul + uint64_t(b) * out_bs : nullptr;
+        // store bin i (times mul's bin i when fused with a convolution product)
+        auto put = [&](uint32_t i, vec2_t v) { O[i] = M ? cmul_t(v, M[i]) : v; };
         const uint32_t n = 2 * h;
         if (k == 0) {
             vec2_t z0 = Z[0];
-            O[0] = {z0.x + z0.y, real_t(0)};
-            O[h] = {z0.x - z0.y, real_t(0)};
-            if (expand && h > 0) { /* mirror of bin h is itself */ }
+            put(0, {z0.x + z0.y, real_t(0)});
+            put(h, {z0.x - z0.y, real_t(0)});
             continue;
         }
         vec2_t fpk = Z[k];
@@ -170,25 +175,26 @@ __global__ void k_real_post(const vec2_t* __restrict__ z, vec2_t* __restrict__ o
         vec2_t a = {real_t(0.5) * (f1k.x + tw.x), real_t(0.5) * (f1k.y + tw.y)};
         vec2_t bb = {real_t(0.5) * (f1k.x - tw.x), real_t(0.5) * (tw.y - f1k.y)};
         if (2 * k == h) {
-            O[k] = bb;  // both writes land on the same bin; the later one wins
-            if (expand) O[n - k] = {bb.x, -bb.y};
+            put(k, bb);  // both values land on the same bin; the later one wins
+            if (expand) put(n - k, {bb.x, -bb.y});
         } else {
-            O[k] = a;
-            O[h - k] = bb;
+            put(k, a);
+            put(h - k, bb);
             if (expand) {
-                O[n - k] = {a.x, -a.y};
-                O[n - (h - k)] = {bb.x, -bb.y};
+                put(n - k, {a.x, -a.y});
+                put(n - (h - k), {bb.x, -bb.y});
             }
         }
     }
 }
 
 void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32_t h,
-                      uint32_t batch, uint64_t out_bs, int expand, cudaStream_t st) {
+                      uint32_t batch, uint64_t out_bs, int expand, cudaStream_t st,
+                      const vec2_t* mul) {
     uint64_t total = (uint64_t(h / 2) + 1) * batch;
     uint64_t blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    k_real_post<<<uint32_t(blocks), 256, 0, st>>>(z, out, st_tab, h, batch, out_bs, expand);
+    k_real_post<<<uint32_t(blocks), 256, 0, st>>>(z, out, st_tab, h, batch, out_bs, expand, mul);
     note_cuda_error(cudaGetLastError());
     count_launch();
 }

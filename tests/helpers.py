@@ -15,6 +15,15 @@ def tol64(n):
     return 1e-13 * max(np.log2(max(n, 2)), 1.0)
 
 
-# FP32 builds are compared with the FP64 oracle; the reference float build
-# itself reaches ~1.2e-6 on Rader primes.
-TOL32 = 5e-6
+# FP32 builds are compared with the FP64 oracle at the bound the FP32 path is
+# specified to meet, relative L2 error <= 1e-6 (the reference float build
+# itself reaches ~1.2e-6 on Rader primes).
+TOL32 = 1e-6
+
+# The opt-in tensor-core radix-16 stages (KFFT_FLAG_TENSOR_CORES) split the
+# FP32 data and the DFT matrix into two FP16 terms each, about 22 significand
+# bits against FP32's 24, so they do not meet TOL32 on every input: measured
+# 1.05e-6 at 2^24, 1.23e-6 on the high-dynamic-range input at 64 x 2^18 and
+# 1.96e-6 on the Rader prime 65537 (7e-7 and below on the smaller sizes).
+# Their tests hold this looser bound and say so; the default path meets TOL32.
+TOL32_TC = 2.5e-6

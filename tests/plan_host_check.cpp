@@ -35,5 +35,14 @@ int main() {
             for (uint32_t R : kfft::split_passes(n, rmax)) std::printf(" %u", R);
             std::printf("\n");
         }
+    for (uint32_t R : {1u, 2u, 3u, 16u, 32u, 48u, 60u, 72u, 81u, 90u, 96u, 100u, 105u, 108u, 112u,
+                       120u, 126u, 144u, 243u, 250u, 270u, 432u, 486u, 500u, 540u, 567u, 576u,
+                       600u, 630u, 648u, 672u, 700u, 720u, 729u, 750u, 756u, 864u, 945u, 1000u,
+                       1008u, 2048u, 2187u, 3125u, 3888u, 4096u, 4095u, 3003u, 496u, 17u * 27u})
+    {
+        std::printf("radices %u", R);
+        for (uint8_t q : kfft::inner_radices(R)) std::printf(" %u", unsigned(q));
+        std::printf("\n");
+    }
     return 0;
 }

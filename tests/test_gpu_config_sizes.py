@@ -1,0 +1,153 @@
+"""Parity at the full sizes of the benchmarked configurations, against the FP64
+oracle (the reference algorithm restated in C).
+
+FP32 results must stay within relative L2 error 1e-6 of the oracle on the
+same (FP32-rounded) input, sequence by sequence; FP64 results within
+1e-13 * log2(N).  The sizes and inputs follow the benchmark workloads:
+
+* 1D complex FP32: one 2^24-point sequence and 64 sequences of 2^18, re/im
+  iid N(0,1) (seed 3), and the high-dynamic-range input (seed 4): 32 tones
+  per sequence with amplitudes 10^U[-6,0] and random phases, plus N(0, 1e-7^2)
+  noise.  The tones are placed on bins and synthesised with an FP64 inverse
+  FFT, which gives the same kind of signal as a direct sum of exponentials.
+* real FP32 2^22 (4 sequences of the U[-1,1) input, seed 5);
+* 2D complex 8192 x 8192 FP32 and 4096 x 4096 FP64, N(0,1) (seed 6);
+* 2D convolution of a 4096^2 U[0,1) image (seed 7) with a 63 x 63 Gaussian
+  (sigma 8, sum 1), both zero-padded to 4160^2, against the oracle's circular
+  2D convolution of the same padded arrays (the reference's even-length real
+  inverse returns twice the input, and so does the oracle);
+* every sequence of the uneven batch (3,968 FP32 sequences, 281,598,199
+  points).
+"""
+import numpy as np
+import pytest
+
+import kfft_gb300 as K
+from oracle import oracle as O
+from tests.helpers import TOL32, TOL32_TC, rel_l2, tol64
+
+pytestmark = pytest.mark.gpu
+
+
+def _normal(rng, shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+def _hdr(rng, batch, n):
+    """32 tones per row (bins uniform, amplitudes 10^U[-6,0], random phases)
+    plus complex N(0, 1e-7^2) noise."""
+    spec = np.zeros((batch, n), np.complex128)
+    for b in range(batch):
+        f = rng.integers(0, n, 32)
+        amp = 10.0 ** rng.uniform(-6, 0, 32)
+        ph = rng.uniform(0, 2 * np.pi, 32)
+        np.add.at(spec[b], f, amp * np.exp(1j * ph) * n)
+    x = np.fft.ifft(spec, axis=-1)
+    return x + 1e-7 * _normal(rng, (batch, n))
+
+
+def _rows_within(y, ref, tol):
+    errs = [rel_l2(y[b], ref[b]) for b in range(y.shape[0])]
+    return max(errs)
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 24, 1), (1 << 18, 64)])
+@pytest.mark.parametrize("dist", ["normal", "hdr"])
+def test_fp32_large_transforms(libf, n, batch, dist):
+    rng = np.random.default_rng(3 if dist == "normal" else 4)
+    x = (_normal(rng, (batch, n)) if dist == "normal" else _hdr(rng, batch, n)).astype(np.complex64)
+    xr = x.astype(np.complex128)
+    y = libf.fft_cpx(x)
+    ref = O.CpxPlan(n, O.FLAG_NORMAL)(xr).reshape(batch, n)
+    assert _rows_within(y, ref, TOL32) <= TOL32
+    z = libf.fft_cpx(y, K.FLAG_INVERSE)
+    refi = O.CpxPlan(n, O.FLAG_INVERSE)(y.astype(np.complex128)).reshape(batch, n)
+    assert _rows_within(z, refi, TOL32) <= TOL32
+    assert _rows_within(z, xr, 2 * TOL32) <= 2 * TOL32  # round trip
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 24, 1), (1 << 18, 64)])
+def test_fp32_large_tensor_core_variant(libf, n, batch):
+    """The opt-in tensor-core radix-16 stages (FP16 hi+lo split, FP32
+    accumulation) on the same sizes, normal and high-dynamic-range input.
+    They miss the 1e-6 bound here (1.05e-6 at 2^24, 1.23e-6 on the
+    high-dynamic-range input at 64 x 2^18): two FP16 terms carry about 22
+    significand bits.  The test holds them to TOL32_TC and checks that the
+    default path meets TOL32 on the same inputs."""
+    for dist, seed in (("normal", 3), ("hdr", 4)):
+        rng = np.random.default_rng(seed)
+        x = (_normal(rng, (batch, n)) if dist == "normal" else _hdr(rng, batch, n)).astype(np.complex64)
+        ref = O.CpxPlan(n, O.FLAG_NORMAL)(x.astype(np.complex128)).reshape(batch, n)
+        y = libf.fft_cpx(x, K.FLAG_TENSOR_CORES)
+        assert _rows_within(y, ref, TOL32_TC) <= TOL32_TC, dist
+        assert _rows_within(libf.fft_cpx(x), ref, TOL32) <= TOL32, dist
+
+
+def test_fp32_real_2p22(libf):
+    n = 1 << 22
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (4, n)).astype(np.float32)
+    X = libf.rfft(x)
+    ref = np.stack([O.rfft(x[b].astype(np.float64)) for b in range(4)])
+    assert _rows_within(X, ref, TOL32) <= TOL32
+    back = libf.irfft(X, n)
+    # the reference's even-length real inverse returns twice the input
+    assert max(rel_l2(back[b], 2.0 * x[b]) for b in range(4)) <= 2 * TOL32
+
+
+def test_fp32_2d_8192(libf):
+    rng = np.random.default_rng(6)
+    a = _normal(rng, (8192, 8192)).astype(np.complex64)
+    y = libf.fft2_cpx(a)
+    ref = O.fft2_cpx(a.astype(np.complex128))
+    assert rel_l2(y, ref) <= TOL32
+    z = libf.fft2_cpx(y, K.FLAG_INVERSE)
+    assert rel_l2(z, a) <= 2 * TOL32
+
+
+def test_fp64_2d_4096(lib):
+    rng = np.random.default_rng(6)
+    a = _normal(rng, (4096, 4096))
+    y = lib.fft2_cpx(a)
+    ref = O.fft2_cpx(a)
+    assert rel_l2(y, ref) <= tol64(4096 * 4096)
+    z = lib.fft2_cpx(y, K.FLAG_INVERSE)
+    assert rel_l2(z, a) <= tol64(4096 * 4096)
+
+
+def test_fp32_conv2d_4096_gaussian(libf):
+    M = 4160
+    rng = np.random.default_rng(7)
+    img = np.zeros((M, M), np.float32)
+    img[:4096, :4096] = rng.uniform(0, 1, (4096, 4096))
+    g = np.arange(63) - 31
+    k = np.exp(-(g[:, None] ** 2 + g[None, :] ** 2) / (2 * 8.0 ** 2))
+    ker = np.zeros((M, M), np.float32)
+    ker[:63, :63] = k / k.sum()
+    got = libf.conv2_scalar(img, ker)
+    ref = O.conv2_scalar(img.astype(np.float64), ker.astype(np.float64))
+    assert rel_l2(got, ref) <= TOL32
+    # the linear convolution sits in the first 4096 + 62 rows and columns
+    assert np.abs(got[4158:, :]).max() <= 1e-5 * np.abs(got).max()
+
+
+def test_fp32_uneven_full_batch(libf):
+    """Every sequence of the benchmark's uneven batch against the oracle."""
+    import bench
+    lengths = np.ascontiguousarray(bench.uneven_lengths())
+    total = int(lengths.sum(dtype=np.int64))
+    rng = np.random.default_rng(2)
+    x = _normal(rng, total).astype(np.complex64)
+    p = libf.L.kfft_config_cpx_uneven(len(lengths), lengths.ctypes.data, 0)
+    assert p, libf.last_error()
+    try:
+        y = np.empty_like(x)
+        assert libf.L.kfft_eval_cpx_uneven(p, x.ctypes.data, y.ctypes.data) == 0
+    finally:
+        libf.L.kfft_release_uneven(p)
+    ref = O.fft_uneven(lengths, x.astype(np.complex128))
+    offs = np.concatenate([[0], np.cumsum(lengths.astype(np.int64))])
+    errs = np.array([rel_l2(y[offs[i]:offs[i + 1]], ref[offs[i]:offs[i + 1]])
+                     for i in range(len(lengths))])
+    worst = int(np.argmax(errs))
+    assert errs.max() <= TOL32, (int(lengths[worst]), float(errs.max()))

@@ -90,6 +90,44 @@ def test_queue_wait_gives_up_and_reports(libf, lib):
     assert rel_l2(lib.fft_cpx(x), O.fft_cpx(x)) <= 1e-13 * 6
 
 
+def test_bulk_copy_wait_gives_up_and_reports(libf):
+    """The FP32 single-pass kernel that receives its tiles by bulk copy waits
+    on each copy with a bounded poll loop.  With the limit lowered to one
+    non-blocking poll, the first wait of every CTA runs out on a valid copy
+    still in flight: the CTA records the failure, waits (with the default
+    limit) for that copy to land and stops.  The synchronous call must then
+    return KFFT_RET_BUFFER_FAIL, the asynchronous one must report it through
+    kfft_gb300_check_waits, and with the default limit restored the same
+    calls succeed and match the FP64 oracle in the same context."""
+    n, batch = 4096, 4096  # 2^24 points: more tiles than resident CTAs, so the bulk path runs
+    rng = np.random.default_rng(31)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    p = libf._plan("kfft_config_cpx", n, 0)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    try:
+        torch.cuda.synchronize()
+        libf.L.kfft_gb300_set_bulk_wait_polls(1)
+        try:
+            assert libf.L.kfft_eval_cpx_batch(p, xd.data_ptr(), yd.data_ptr(), batch) == K.RET_BUFFER_FAIL
+            assert "wait" in libf.last_error()
+            assert libf.L.kfft_eval_cpx_async(p, xd.data_ptr(), yd.data_ptr(), batch, None) == 0
+            assert libf.L.kfft_gb300_check_waits(None) == 1
+            assert libf.L.kfft_gb300_check_waits(None) == 0  # the record was cleared
+        finally:
+            libf.L.kfft_gb300_set_bulk_wait_polls(0)
+        yd.zero_()
+        torch.cuda.synchronize()
+        assert libf.L.kfft_eval_cpx_batch(p, xd.data_ptr(), yd.data_ptr(), batch) == 0
+        assert libf.L.kfft_eval_cpx_async(p, xd.data_ptr(), yd.data_ptr(), batch, None) == 0
+        assert libf.L.kfft_gb300_check_waits(None) == 0
+        y = yd.cpu().numpy()
+        for b in (0, 1, batch // 2, batch - 1):
+            assert rel_l2(y[b], O.fft_cpx(x[b])) <= TOL32
+    finally:
+        libf.cleanup(p)
+
+
 @pytest.mark.parametrize("logn", list(range(4, 13)) + [13, 16, 20, 22])
 def test_pipelined_power_of_two_passes(libf, logn):
     """FP32 power-of-two passes run as resident CTAs that loop over many

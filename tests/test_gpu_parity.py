@@ -1,5 +1,5 @@
 """GPU parity of the engine through its C ABI against the reference fixtures
-and the FP64 oracle.  FP64: rel-L2 <= 1e-13*log2(N); FP32: rel-L2 <= 5e-6."""
+and the FP64 oracle.  FP64: rel-L2 <= 1e-13*log2(N); FP32: rel-L2 <= 1e-6."""
 import json
 import os
 
@@ -281,7 +281,10 @@ def test_uneven_workload_subset(precision):
 @pytest.mark.parametrize("n,batch", [(16, 64), (256, 16), (4096, 8), (65536, 2), (1 << 18, 1),
                                      (1 << 20, 1), (3 * 4096, 2), (1000, 4)])
 def test_tensor_core_radix16_path(libf, n, batch):
-    """FP32 build with KFFT_FLAG_TENSOR_CORES: FP16 split hi+lo radix-16 stages."""
+    """FP32 build with KFFT_FLAG_TENSOR_CORES: FP16 split hi+lo radix-16
+    stages, held to the plain FP32 bound at these sizes (up to 2^20; the
+    larger benchmark sizes, where the split's 22 bits miss it, are in
+    test_gpu_config_sizes.py)."""
     rng = np.random.default_rng(n)
     x = cx(rng, batch, n).astype(np.complex64)
     ref = O.fft_cpx(x.astype(np.complex128))
@@ -289,9 +292,9 @@ def test_tensor_core_radix16_path(libf, n, batch):
     y = np.empty_like(x)
     assert libf.L.kfft_eval_cpx_batch(p, x.ctypes.data, y.ctypes.data, batch) == 0
     libf.cleanup(p)
-    assert rel_l2(y, ref) <= 2e-6
+    assert rel_l2(y, ref) <= TOL32
     pi = libf.L.kfft_config_cpx(n, 1 | (1 << 8), None, None)
     z = np.empty_like(x)
     assert libf.L.kfft_eval_cpx_batch(pi, y.ctypes.data, z.ctypes.data, batch) == 0
     libf.cleanup(pi)
-    assert rel_l2(z, x) <= 4e-6
+    assert rel_l2(z, x) <= 2 * TOL32

@@ -61,21 +61,53 @@ def split(L, rmax):
     return [1 << e for e in best[1]]
 
 
+# butterfly flops of each register radix, plus r-1 twiddle products, per point
+BFLY = {2: 4, 3: 16, 4: 16, 5: 40, 6: 44, 7: 72, 8: 52, 9: 120, 10: 100, 11: 140, 12: 112,
+        13: 190, 14: 172, 15: 200, 16: 144}
+
+
+def _flops(r):
+    return (BFLY.get(r, 4.0 * r * r) + 6.0 * (r - 1)) / r
+
+
 def radices(R):
-    r, e2 = [], 0
-    while R % 2 == 0:
-        R //= 2
-        e2 += 1
-    r += [16] * (e2 // 4)
-    if e2 % 4:
-        r.append(1 << (e2 % 4))
-    p = 3
-    while R > 1:
-        while R % p == 0:
-            r.append(p)
-            R //= p
-        p += 2
-    return r
+    """Inner stages of a tile of R points: powers of two as 16s then 8/4/2;
+    otherwise the fewest stages from radices 2..16 (ties: least estimated
+    flops), largest first, with prime factors 17..31 as stages of their own."""
+    if R >= 2 and R & (R - 1) == 0:
+        e2 = R.bit_length() - 1
+        return [16] * (e2 // 4) + ([1 << (e2 % 4)] if e2 % 4 else [])
+    big, rest, p = [], R, 2
+    while p * p <= rest:
+        while rest % p == 0:
+            if p > 16:
+                big.append(p)
+            rest //= p
+        p += 1
+    # `rest` now holds at most one prime left over; recompute the small part
+    small = R
+    for q in big:
+        small //= q
+    if rest > 16:
+        big.append(rest)
+        small //= rest
+
+    from functools import lru_cache
+
+    @lru_cache(maxsize=None)
+    def best(d):
+        if d == 1:
+            return (0, 0.0, ())
+        out = None
+        for q in range(16, 1, -1):
+            if d % q == 0:
+                s, f, seq = best(d // q)
+                cand = (s + 1, f + _flops(q), seq + (q,))
+                if out is None or cand[0] < out[0] or (cand[0] == out[0] and cand[1] < out[1] - 1e-9):
+                    out = cand
+        return out
+
+    return sorted(best(small)[2], reverse=True) + big
 
 
 def pad(i):
@@ -220,3 +252,22 @@ def test_bluestein_lengths_match_restatement(printed):
         assert m == bluestein(2 * n - 1), (n, m)
         assert m >= 2 * n - 1
     assert got[999983] == 1 << 21  # over the nearest 7-smooth length, 2,000,000
+
+
+def test_inner_radix_schedules_match_restatement(printed):
+    rows = [r for r in printed if r[0] == "radices"]
+    assert len(rows) >= 40
+    for r in rows:
+        R = int(r[1])
+        got = [int(v) for v in r[2:]]
+        assert got == radices(R), r
+        prod = 1
+        for q in got:
+            prod *= q
+        assert prod == R
+    got = {int(r[1]): [int(v) for v in r[2:]] for r in rows}
+    assert got[729] == [9, 9, 9]           # six radix-3 stages before
+    assert got[4096] == [16, 16, 16]       # the compile-time bodies' schedule
+    assert got[2048] == [16, 16, 8]
+    assert len(got[756]) == 3              # 4 * 27 * 7: five stages before
+    assert got[31 * 16] == [16, 31]
