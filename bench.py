@@ -657,7 +657,7 @@ def run_reference(args, ws, rank):
     class _NoLib:
         L = None
     wl = make_workload(args.workload, _NoLib(), need_lib=False, subset=args.subset,
-                       precision=args.precision)
+                       precision=args.precision, batch=args.batch)
     threads = os.cpu_count() or 1
     if isinstance(wl, Uneven):
         import types
@@ -770,12 +770,18 @@ def run_learned_planner(args):
     print(json.dumps(line), flush=True)
 
 
-def make_workload(name, lib, need_lib=True, subset=1, precision="float"):
+def make_workload(name, lib, need_lib=True, subset=1, precision="float", batch=0):
     if name in UNIFORM_WORKLOADS:
-        return UNIFORM_WORKLOADS[name](lib)
-    if name in CONFIG4_WORKLOADS:
-        return CONFIG4_WORKLOADS[name](lib)
-    return Uneven(lib, precision=precision, subset=subset)
+        wl = UNIFORM_WORKLOADS[name](lib)
+    elif name in CONFIG4_WORKLOADS:
+        wl = CONFIG4_WORKLOADS[name](lib)
+    else:
+        return Uneven(lib, precision=precision, subset=subset)
+    if batch and hasattr(wl, "B"):
+        # profiling only: fewer sequences of the same length (a small ncu case)
+        wl.name = wl.name.replace(f"batch {wl.B}", f"batch {batch}")
+        wl.B = batch
+    return wl
 
 
 def main():
@@ -792,6 +798,8 @@ def main():
     ap.add_argument("--tune-db", default="",
                     help="learned_planner: write the tuning table (JSON) and model here")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="profiling only: sequences per step of a uniform or real workload")
     ap.add_argument("--subset", type=int, default=1,
                     help="profiling only: keep every k-th sequence of the uneven batch")
     ap.add_argument("--precision", default="float", choices=["float", "double"],
@@ -817,9 +825,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    probe = make_workload(args.workload, None, subset=args.subset, precision=args.precision)
+    probe = make_workload(args.workload, None, subset=args.subset, precision=args.precision,
+                          batch=args.batch)
     lib = kfft_gb300.load(probe.precision)
-    wl = make_workload(args.workload, lib, subset=args.subset, precision=args.precision)
+    wl = make_workload(args.workload, lib, subset=args.subset, precision=args.precision,
+                       batch=args.batch)
     nbuf = rotating_buffers(wl)
     wl.setup(torch, dev, nbuf)
     stream = torch.cuda.Stream(device=dev)

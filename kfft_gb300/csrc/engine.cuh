@@ -72,25 +72,6 @@ enum : uint8_t {
                        // layout (the other operand's spectrum of a convolution)
 };
 
-// Where a fused convolution pass (PassDesc::fuse) stores its result: the
-// first pass of the inverse transform, whose lanes are the forward last
-// pass's lanes (element j*R + r of sequence b), with that pass's epilogue
-// (EPI_NONE, EPI_CHIRP or EPI_RADER_INV when the inverse has one pass only).
-struct FuseTail {
-    vec2_t* out;
-    uint64_t out_bs;
-    uint32_t out_es;
-    uint8_t epi_op;
-    const vec2_t* epi_tab;
-    const uint32_t* epi_perm;
-    uint32_t epi_bound;
-    const vec2_t* aux_in;
-    vec2_t* aux_out;
-    uint64_t aux_out_bs;
-    uint32_t aux_out_es;
-    real_t scale;
-};
-
 struct PassDesc {
     const vec2_t* in;
     vec2_t* out;
@@ -132,14 +113,6 @@ struct PassDesc {
     uint64_t aux_in_bs, aux_out_bs;
     uint32_t aux_out_es;
     real_t scale;
-    // Fused convolution pass: after its R-point DFTs (the last pass of a
-    // forward transform) each value is multiplied by the epilogue's spectrum
-    // (EPI_MUL or EPI_RADER_FWD) and conjugated in shared memory, the same
-    // inner stages run again (an R-point forward DFT of the conjugate is the
-    // conjugate of the inverse DFT) and the conjugated result goes to `tail`:
-    // the first pass of the inverse transform, one HBM round trip saved.
-    uint8_t fuse;
-    FuseTail tail;
 };
 
 // ---- device tables -----------------------------------------------------
@@ -218,11 +191,16 @@ struct DeviceArena;  // device memory owned by a plan tree
 struct PlanVariant {
     uint32_t rmax = KFFT_PLAN_RMAX;  // largest pass length of a multi-pass split
     uint32_t lanes = 0;          // lanes of multi-pass tiles (0: precision default)
+    uint32_t lanes_mul = 1;      // multiplier on the default lanes of multi-pass tiles
+    uint32_t single_div = 1;     // divisor on the default lanes of single-pass tiles
     uint32_t single_cap = 4096;  // longest length run as one fused pass
+    bool reverse = false;        // multi-pass splits run longest pass last
+    bool no_rader = false;       // primes through Bluestein even where Rader applies
     bool no_fused = false;       // shared-memory ping-pong tiles only
     bool tc = false;             // radix-16 stages on tensor cores (FP32 build)
 };
-constexpr uint32_t kPlanVariants = 6;
+// Variants 0..kPlanVariants-1; the tensor-core variant is always the last.
+constexpr uint32_t kPlanVariants = 10;
 PlanVariant plan_variant(uint32_t index);
 // the variant the tuning table records for (nfft, flags), -1 if none
 int tuned_plan_variant(uint32_t nfft, uint32_t flags);
@@ -284,11 +262,8 @@ std::string describe(const FftPlan& p);
 // Device workspace (bytes) the plan needs for `batch` sequences.
 size_t workspace_bytes(const FftPlan& p, uint32_t batch);
 // Appends the passes computing out = FFT(in) * scale to `descs`.
-// With `fuse`, the forward last pass and the inverse first pass of a Rader
-// or Bluestein convolution become one fused pass where they can.
 bool build_passes(const FftPlan& p, const vec2_t* in, const Layout& lin, vec2_t* out,
-                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs,
-                  bool fuse = true);
+                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs);
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st);
 // Descriptor of pass `pass` of a DIRECT plan (no fused element operations).
 // Start of chunk i (i = 0..k; chunk k's start is `total`) when `total` units

@@ -621,12 +621,7 @@ __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x,
 // (with the epilogue), and only the exchanges between inner passes go through
 // one shared-memory buffer (read all, barrier, write all, barrier).
 // ---------------------------------------------------------------------------
-// Where a stage of the register tile reads or writes: shared memory, global
-// memory (the pass's prologue / epilogue), or, in a fused convolution pass,
-// shared memory through the spectrum product and a conjugation (IO_MID, the
-// forward half's last stage) and global memory through the tail store with a
-// conjugation (IO_TAIL, the inverse half's last stage).
-enum : int { IO_SMEM = 0, IO_GLOBAL = 1, IO_MID = 2, IO_TAIL = 3 };
+enum : int { IO_SMEM = 0, IO_GLOBAL = 1 };
 
 // v[q] *= W^(q*step) for q = 1..P-1, W^i = tw[i].  FP64 loads every factor
 // (the FP64 pipe, not the loads, bounds it).  FP32 loads the four anchors
@@ -659,44 +654,6 @@ __device__ __forceinline__ void apply_inner_twiddles(vec2_t* v, const vec2_t* __
 #endif
 #pragma unroll
     for (int q = 1; q < P; ++q) v[q] = cmul(v[q], __ldg(&tw[q * step]));
-}
-
-__device__ __forceinline__ vec2_t conj2(vec2_t a) { return {a.x, -a.y}; }
-
-// Spectrum product of a fused convolution pass at forward output index k of
-// sequence b (EPI_MUL, or EPI_RADER_FWD with its bin-0 bookkeeping), returned
-// conjugated for the inverse half.
-__device__ __forceinline__ vec2_t fuse_mid(const PassDesc& d, uint32_t b, uint32_t k, vec2_t v) {
-    if (d.epi_op == EPI_RADER_FWD && k == 0) {
-        const vec2_t x0 = __ldcg(&d.aux_in[b * d.aux_in_bs]);
-        d.aux_out[2 * uint64_t(b)] = x0;
-        d.aux_out[2 * uint64_t(b) + 1] = cadd(x0, v);
-    }
-    return conj2(cmul(v, __ldg(&d.epi_tab[k])));
-}
-
-// Store of a fused convolution pass: element k of sequence b of the inverse
-// transform's first pass, after undoing the conjugation, through that pass's
-// epilogue (the cases an inverse first pass can carry).
-__device__ __forceinline__ void store_tail(const FuseTail& t, uint32_t b, uint32_t k, vec2_t v) {
-    v = conj2(v);
-    switch (t.epi_op) {
-        case EPI_CHIRP:
-            if (k < t.epi_bound)
-                t.out[b * t.out_bs + uint64_t(k) * t.out_es] = cscale(cmul(v, __ldg(&t.epi_tab[k])), t.scale);
-            break;
-        case EPI_RADER_INV: {
-            const vec2_t x0 = __ldcg(&t.aux_in[2 * uint64_t(b)]);
-            const uint32_t idx = __ldg(&t.epi_perm[k]);
-            vec2_t* o = t.aux_out + b * t.aux_out_bs;
-            o[uint64_t(idx) * t.aux_out_es] = cscale(cadd(v, x0), t.scale);
-            if (k == 0) o[0] = cscale(__ldcg(&t.aux_in[2 * uint64_t(b) + 1]), t.scale);
-            break;
-        }
-        default:
-            t.out[b * t.out_bs + uint64_t(k) * t.out_es] = cscale(v, t.scale);
-            break;
-    }
 }
 
 // The P inputs of one butterfly of the first inner pass, straight from global
@@ -813,7 +770,7 @@ __device__ __forceinline__ void fused_store(const PassDesc& d, uint32_t bs, uint
 // butterfly at a time from `src` (global memory on the first pass, else a
 // shared buffer) and writes it to `dst` (global memory on the last pass, else
 // the other shared buffer).
-template <int P, bool INV, bool FUSE>
+template <int P, bool INV>
 __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& st,
                                            const vec2_t* src, vec2_t* dst, uint32_t lane0,
                                            uint32_t total, int sio, int dio) {
@@ -821,7 +778,6 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
     const uint32_t items = d.C * m;
     const bool cfast = (sio == IO_GLOBAL) ? (d.load_mode == MODE_LANE)
                                           : ((dio == IO_GLOBAL) ? (d.store_mode == MODE_LANE) : false);
-    const bool need_lane = sio == IO_GLOBAL || dio != IO_SMEM;
     for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
         uint32_t c, jj;
         if (cfast) {
@@ -834,7 +790,7 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         const uint32_t g = lane0 + c;
         uint32_t bs = 0, j = 0;
         const bool live = g < total;
-        if (need_lane && live) {
+        if ((sio == IO_GLOBAL || dio == IO_GLOBAL) && live) {
             if (d.order == ORDER_J) {
                 bs = fdiv(g, d.div_lanes_j);
                 j = g - bs * d.lanes_j;
@@ -863,22 +819,8 @@ __device__ __forceinline__ void fused_pass(const PassDesc& d, const InnerStep& s
         if (dio == IO_SMEM) {
 #pragma unroll
             for (int q = 0; q < P; ++q) dst[c * d.lane_stride + pad(ob + q * st.ns)] = v[q];
-        } else if (FUSE && dio == IO_MID) {
-            // forward output index k = j + r Ns of the last pass (blo = 0)
-#pragma unroll
-            for (int q = 0; q < P; ++q) {
-                const uint32_t r = ob + q * st.ns;
-                dst[c * d.lane_stride + pad(r)] =
-                    live ? fuse_mid(d, bs, j + r * d.Ns, v[q]) : vec2_t{real_t(0), real_t(0)};
-            }
         } else if (live) {
-            if (FUSE && dio == IO_TAIL) {
-                // the inverse's first pass: lane j holds elements j R + r
-#pragma unroll
-                for (int q = 0; q < P; ++q) store_tail(d.tail, bs, j * d.R + ob + q * st.ns, v[q]);
-            } else {
-                fused_store<P>(d, bs, j, ob, st.ns, v);
-            }
+            fused_store<P>(d, bs, j, ob, st.ns, v);
         }
     }
 }
@@ -1439,26 +1381,26 @@ __device__ __forceinline__ void tile_loop_bulk(const PassDesc& d, unsigned char*
 }
 #endif
 
-template <bool INV, bool FUSE>
+template <bool INV>
 __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const InnerStep& st,
                                                const vec2_t* src, vec2_t* dst, uint32_t lane0,
                                                uint32_t total, int sio, int dio) {
     switch (P) {
-        case 2: fused_pass<2, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 3: fused_pass<3, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 4: fused_pass<4, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 5: fused_pass<5, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 7: fused_pass<7, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 6: fused_pass<6, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 8: fused_pass<8, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 9: fused_pass<9, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 10: fused_pass<10, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 11: fused_pass<11, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 12: fused_pass<12, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 13: fused_pass<13, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 14: fused_pass<14, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 15: fused_pass<15, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
-        case 16: fused_pass<16, INV, FUSE>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 2: fused_pass<2, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 3: fused_pass<3, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 4: fused_pass<4, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 5: fused_pass<5, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 7: fused_pass<7, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 6: fused_pass<6, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 8: fused_pass<8, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 9: fused_pass<9, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 10: fused_pass<10, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 11: fused_pass<11, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 12: fused_pass<12, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 13: fused_pass<13, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 14: fused_pass<14, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 15: fused_pass<15, INV>(d, st, src, dst, lane0, total, sio, dio); break;
+        case 16: fused_pass<16, INV>(d, st, src, dst, lane0, total, sio, dio); break;
         default: break;
     }
 }
@@ -1471,9 +1413,7 @@ __device__ __forceinline__ void fused_dispatch(int P, const PassDesc& d, const I
 // the pass kernel launches those as kernels of their own and leaves it off.
 // TC: keep the tensor-core radix-16 stage; the queue kernel leaves it off
 // (its planner clears d.tc) to keep its instruction footprint small.
-// FUSE: run fused convolution passes (PassDesc::fuse); the queue kernel
-// leaves it off (its planner does not fuse) to keep its body small.
-template <bool INV, bool SPEC = true, bool TC = true, bool FUSE = true>
+template <bool INV, bool SPEC = true, bool TC = true>
 __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra& x, uint32_t tile,
                                               vec2_t* sm) {
     const uint32_t total = d.batch * d.lanes_j;
@@ -1520,22 +1460,16 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
         Gm = dft16_frag<INV>(2);
     }
 #endif
-    // a fused convolution pass runs the inner stages twice: the forward
-    // half ends in shared memory (IO_MID), the inverse half in the tail store
-    const bool fuse = FUSE && d.fuse;
-    const int ns_total = fuse ? 2 * np : np;
-    for (int s = 0; s < ns_total; ++s) {
-        const int p = s < np ? s : s - np;
-        const bool last = (s + 1 == ns_total);
-        vec2_t* dst = last ? nullptr : ((s % 2 == 0) ? bufA : bufB);
-        const int sio = s == 0 ? IO_GLOBAL : IO_SMEM;
-        const int dio = last ? (fuse ? IO_TAIL : IO_GLOBAL) : (fuse && s == np - 1 ? IO_MID : IO_SMEM);
+    for (int p = 0; p < np; ++p) {
+        const bool last = (p + 1 == np);
+        vec2_t* dst = last ? nullptr : ((p % 2 == 0) ? bufA : bufB);
+        const int sio = p == 0 ? IO_GLOBAL : IO_SMEM, dio = last ? IO_GLOBAL : IO_SMEM;
 #if defined(KFFT_HALF_SCALAR)
         if (TC && d.tc && d.rad[p] == 16)
             tc_pass16<INV>(d, x.step[p], src, dst, lane0, total, sio, dio, Fr, Fi, Gm);
         else
 #endif
-            fused_dispatch<INV, FUSE>(d.rad[p], d, x.step[p], src, dst, lane0, total, sio, dio);
+            fused_dispatch<INV>(d.rad[p], d, x.step[p], src, dst, lane0, total, sio, dio);
         if (!last) __syncthreads();
         src = dst;
     }

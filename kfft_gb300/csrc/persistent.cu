@@ -46,8 +46,8 @@ __global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent
         __syncthreads();
         if (s_ok) {
             const PassExtra& x = extras[q.desc];
-            if (s_desc.inv) tile_body_reg<true, true, false, false>(s_desc, x, q.tile, buf);
-            else tile_body_reg<false, true, false, false>(s_desc, x, q.tile, buf);
+            if (s_desc.inv) tile_body_reg<true, true, false>(s_desc, x, q.tile, buf);
+            else tile_body_reg<false, true, false>(s_desc, x, q.tile, buf);
         }
         __threadfence();
         __syncthreads();

@@ -211,6 +211,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
         else Rs = split_passes(N, std::min(kMultiRmax, V.rmax));
     }
     if (Rs.empty()) return false;
+    if (V.reverse) std::reverse(Rs.begin(), Rs.end());
     std::map<uint32_t, const vec2_t*> inner;
     uint32_t Ns = 1;
     for (uint32_t R : Rs) {
@@ -248,21 +249,6 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     return true;
 }
 
-// Reverses the pass order of a DIRECT plan (any order is a valid Stockham
-// split; Ns of each pass is the product of the lengths before it).  The
-// inverse transform of a convolution runs its passes in the reverse order of
-// the forward's, so that its first pass has the forward last pass's length and
-// lanes, which lets the two fuse into one pass (fuse_convolution_passes).
-static void reverse_passes(FftPlan* P) {
-    if (!P || P->method != METHOD_DIRECT || P->passes.size() < 2) return;
-    std::reverse(P->passes.begin(), P->passes.end());
-    uint32_t Ns = 1;
-    for (PassSpec& s : P->passes) {
-        s.Ns = Ns;
-        Ns *= s.R;
-    }
-}
-
 // runs `plan` once on device data to precompute a spectrum (contiguous, batch 1)
 static bool transform_once(const FftPlan& plan, const vec2_t* in, vec2_t* out, cudaStream_t st) {
     size_t ws_bytes = workspace_bytes(plan, 1);
@@ -292,14 +278,20 @@ static bool transform_once(const FftPlan& plan, const vec2_t* in, vec2_t* out, c
     return ok;
 }
 
+// The tuner's search space: each variant changes one planning decision of
+// the default rule (variant 0); all compute the same transform.
 PlanVariant plan_variant(uint32_t index) {
     PlanVariant v;
     switch (index) {
-        case 1: v.rmax = 512; break;
-        case 2: v.rmax = 256; v.lanes = 16; break;
-        case 3: v.no_fused = true; break;
-        case 4: v.single_cap = 1024; break;
-        case 5: v.tc = true; break;
+        case 1: v.rmax = 512; break;                  // shorter passes, more of them
+        case 2: v.rmax = 256; v.lanes = 16; break;     // short passes, wide tiles
+        case 3: v.no_fused = true; break;              // shared-memory tiles
+        case 4: v.single_cap = 1024; break;            // split lengths above 1024
+        case 5: v.reverse = true; break;               // pass order reversed
+        case 6: v.lanes_mul = 2; break;                // twice the lanes per multi-pass tile
+        case 7: v.single_div = 2; break;               // half the lanes per single-pass tile
+        case 8: v.no_rader = true; break;              // Bluestein instead of Rader
+        case 9: v.tc = true; break;                    // tensor-core radix-16 stages
         default: break;
     }
     return v;
@@ -323,7 +315,7 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
         }
         return P;
     }
-    if (is_prime(N) && is_direct_length(N - 1, max_prime)) {
+    if (is_prime(N) && is_direct_length(N - 1, max_prime) && !var.no_rader) {
         // ---- Rader: X[g^-q] = x0 + sum_j x[g^j] W^(g^(j-q)) ------------------
         P->method = METHOD_RADER;
         const uint32_t L = N - 1;
@@ -357,7 +349,6 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
             delete P;
             return nullptr;
         }
-        reverse_passes(P->sub_inv);
         // kernel s[j] = W_N^(g^-j) in the direction of the plan, spectrum / L
         gen_rader_kernel(kern, dip, N, sign, st);
         if (!transform_once(*P->sub_fwd, kern, spec, st)) {
@@ -391,7 +382,6 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
         delete P;
         return nullptr;
     }
-    reverse_passes(P->sub_inv);
     if (!transform_once(*P->sub_fwd, filt, spec, st)) {
         delete P;
         return nullptr;
@@ -427,6 +417,8 @@ std::string describe(const FftPlan& p) {
     }
     // variant knobs that change the kernels but not the pass split
     if (p.var.lanes && p.passes.size() > 1) o << " | lanes=" << p.var.lanes;
+    if (p.var.lanes_mul > 1 && p.passes.size() > 1) o << " | lanes x" << p.var.lanes_mul;
+    if (p.var.single_div > 1 && p.passes.size() == 1) o << " | tiles /" << p.var.single_div;
     if (p.var.no_fused) o << " | smem";
     if (p.tc && has16) o << " | tc";
     return o.str();
@@ -502,7 +494,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.load_mode = MODE_LANE;
         d.store_mode = MODE_LANE;
     } else if (d.lanes_j == 1) {
-        const uint32_t target = (sizeof(vec2_t) == 8) ? 4096 : 2048;
+        const uint32_t target = ((sizeof(vec2_t) == 8) ? 4096 : 2048) / std::max<uint32_t>(1, P.var.single_div);
         C = std::max<uint32_t>(1, std::min(target / std::max<uint32_t>(s.R, 1), cap / std::max<uint32_t>(s.R, 1)));
         C = std::min(C, d.batch);
         d.load_mode = MODE_ELEM;
@@ -515,7 +507,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         const uint32_t share = lane_share(s.R);
         for (uint8_t r : s.radices)
             want = std::max<uint32_t>(want, (kPassThreads * r + share * s.R - 1) / (share * s.R));
-        C = std::min(P.var.lanes ? P.var.lanes : want, d.lanes_j);
+        C = std::min(P.var.lanes ? P.var.lanes : want * std::max<uint32_t>(1, P.var.lanes_mul), d.lanes_j);
         d.load_mode = MODE_LANE;
         d.store_mode = (s.Ns == 1) ? MODE_ELEM : MODE_LANE;
     }
@@ -645,59 +637,8 @@ static bool build_direct_passes(const FftPlan& P, const vec2_t* in, const Layout
 // lanes: f's tile then runs its R-point DFTs, the product, and the inverse
 // R-point DFTs of the same lanes (as conjugated forward DFTs), and stores
 // where i would have.  Returns false (and leaves both) when they do not match.
-static bool fuse_convolution_passes(PassDesc& f, const PassDesc& i);
-
-// Fuses descs[k] (the forward's last pass, which wrote `A`) with descs[k+1]
-// (the inverse's first pass) when fuse_convolution_passes allows it.  The
-// inverse reuses the forward's scratch, so the inverse's first scratch
-// buffer can be the very buffer the fused pass reads (a two-pass forward
-// reads its first scratch buffer there): tiles would then overwrite input
-// other tiles have not read yet.  In that case the fused pass writes to `A`,
-// which the forward no longer writes, and the inverse's next pass reads it
-// there (A has the same per-sequence layout as the scratch buffers).
-static void fuse_at(std::vector<PassDesc>& descs, size_t k, vec2_t* A) {
-    if (k + 1 >= descs.size() || !fuse_convolution_passes(descs[k], descs[k + 1])) return;
-    vec2_t* const old_out = descs[k].tail.out;
-    const bool aliases = old_out == descs[k].in;
-    descs.erase(descs.begin() + long(k) + 1);
-    if (aliases) {
-        descs[k].tail.out = A;
-        if (k + 1 < descs.size() && descs[k + 1].in == old_out) descs[k + 1].in = A;
-    }
-}
-
-static bool fuse_convolution_passes(PassDesc& f, const PassDesc& i) {
-    if (!f.regmode || !i.regmode || f.tc || i.tc) return false;
-    if (f.R != i.R || f.R < 2 || f.lanes_j != i.lanes_j || f.batch != i.batch) return false;
-    if (f.order != ORDER_J || i.order != ORDER_J || i.Ns != 1 || f.Ns != f.lanes_j) return false;
-    if (i.pro_op != PRO_NONE || (f.epi_op != EPI_MUL && f.epi_op != EPI_RADER_FWD)) return false;
-    if (f.nrad != i.nrad) return false;
-    for (int k = 0; k < f.nrad; ++k)
-        if (f.rad[k] != i.rad[k]) return false;
-    f.fuse = 1;
-    f.spec = 0;  // the generic body runs the doubled stage list
-    FuseTail& t = f.tail;
-    t.out = i.out;
-    t.out_bs = i.out_bs;
-    t.out_es = i.out_es;
-    t.epi_op = i.epi_op;
-    t.epi_tab = i.epi_tab;
-    t.epi_perm = i.epi_perm;
-    t.epi_bound = i.epi_bound;
-    t.aux_in = i.aux_in;
-    t.aux_out = i.aux_out;
-    t.aux_out_bs = i.aux_out_bs;
-    t.aux_out_es = i.aux_out_es;
-    t.scale = i.scale;
-    // 2 * nrad stages: one exchange buffer for two stages, two for more
-    const uint32_t nbuf = 2 * f.nrad >= 3 ? 2u : 1u;
-    f.smem_bytes = nbuf * (f.C * f.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
-    return true;
-}
-
 bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t* out,
-                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs,
-                  bool fuse) {
+                  const Layout& lout, real_t scale, Workspace& ws, std::vector<PassDesc>& descs) {
     if (P.N == 0) return true;
     if (uint64_t(lin.batch) * P.N >= (uint64_t(1) << 32) && P.method == METHOD_DIRECT &&
         P.passes.size() > 1)
@@ -722,15 +663,12 @@ bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t*
         Layout lx = lin;  // the input seen as length-L sequences with the caller's strides
         const size_t mark = ws.used;
         if (!build_direct_passes(*P.sub_fwd, in, lx, A, la, real_t(1), ff, ws, descs)) return false;
-        const size_t last_fwd = descs.size() - 1;
         ws.used = mark;  // the inverse reuses the forward's scratch (stream ordered)
         Fuse fi;
         fi.epi_op = EPI_CHIRP;
         fi.epi_tab = P.chirp;
         fi.epi_bound = P.N;
-        if (!build_direct_passes(*P.sub_inv, A, la, out, lout, scale, fi, ws, descs)) return false;
-        if (fuse) fuse_at(descs, last_fwd, A);
-        return true;
+        return build_direct_passes(*P.sub_inv, A, la, out, lout, scale, fi, ws, descs);
     }
     // Rader
     vec2_t* pairs = ws.take(size_t(2) * B);
@@ -745,7 +683,6 @@ bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t*
     ff.aux_out = pairs;
     const size_t mark = ws.used;
     if (!build_direct_passes(*P.sub_fwd, in, lin, A, la, real_t(1), ff, ws, descs)) return false;
-    const size_t last_fwd = descs.size() - 1;
     ws.used = mark;  // the inverse reuses the forward's scratch (stream ordered)
     Fuse fi;
     fi.epi_op = EPI_RADER_INV;
@@ -754,9 +691,7 @@ bool build_passes(const FftPlan& P, const vec2_t* in, const Layout& lin, vec2_t*
     fi.aux_out = out;
     fi.aux_out_bs = lout.bs;
     fi.aux_out_es = lout.es;
-    if (!build_direct_passes(*P.sub_inv, A, la, A, la, scale, fi, ws, descs)) return false;
-    if (fuse) fuse_at(descs, last_fwd, A);
-    return true;
+    return build_direct_passes(*P.sub_inv, A, la, A, la, scale, fi, ws, descs);
 }
 
 void run_passes(const std::vector<PassDesc>& descs, cudaStream_t st) {

@@ -115,9 +115,8 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
         l.batch = 1;
         l.bs = n;
         const size_t first = all.size();
-        // the queue kernel runs no fused convolution passes: its body stays small
         if (!build_passes(fp, in + P->offsets[i], l, out + P->offsets[i], l,
-                          scale_for(P->flags, n), ws, all, false))
+                          scale_for(P->flags, n), ws, all))
             return false;
         for (size_t k = first; k < all.size(); ++k) {
             deps.push_back(k == first ? -1 : int32_t(k - 1));

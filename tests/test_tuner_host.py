@@ -24,12 +24,12 @@ def test_factorize_and_inner_length():
 
 
 def test_feature_vector_layout():
-    nvar = 6
+    nvar = 10
     f = T.features(4096, 4096, "float", 3, nvar)
     assert f.dtype == np.float32 and f.shape == (T.N_BASE_FEATURES + nvar,)
     assert f[0] == 12 and f[1] == 12 and f[2] == 1.0
     assert f[3] == 12                                  # exponent of 2
-    assert list(f[-nvar:]) == [0, 0, 0, 1, 0, 0]
+    assert list(f[-nvar:]) == [0, 0, 0, 1, 0, 0, 0, 0, 0, 0]
     g = T.features(65537, 256, "double", 0, nvar)
     assert g[2] == 0.0
     inner = g[3 + len(T.SMALL_PRIMES) + 2:]
