@@ -1116,6 +1116,63 @@ size_t c2d_bytes(const kfft_plan_c2d* p) {
     return r256(workspace_bytes(*gp(p->plan_x), p->y)) + columns_bytes(*gp(p->plan_y), p->x, p->y);
 }
 
+// A 2D complex transform from host memory to host memory whose copy in
+// overlaps the row passes: the rows arrive in chunks, each chunk's row
+// transforms starting as soon as its copy lands.  The column passes need
+// every row, and the copy out (one contiguous copy) waits for them.
+// (Copying column blocks out by pitched copies under the next
+// block's column passes measured slower: 14.1 against 11.6 ms per forward +
+// inverse step of 8192^2 FP32, the single staged call 12.2 ms.)
+constexpr uint32_t k2dRowChunks = 8;
+
+bool c2d_pipelines(const kfft_plan_c2d* p, const void* fin, const void* fout) {
+    const size_t bytes = sizeof(vec2_t) * size_t(p->x) * p->y;
+    return bytes >= (size_t(16) << 20) && p->y >= k2dRowChunks && !is_device_pointer(fin) &&
+           !is_device_pointer(fout);
+}
+
+kfft_return_t c2d_host_pipelined(const kfft_plan_c2d* p, const vec2_t* fin, vec2_t* fout,
+                                 kfft_gpu_plan* g) {
+    cudaSetDevice(current_device());
+    cudaStream_t st = sync_stream();
+    CopyStreams* cs = copy_streams();
+    if (!cs) return KFFT_RET_BUFFER_FAIL;
+    const FftPlan& Px = *gp(p->plan_x);
+    const FftPlan& Py = *gp(p->plan_y);
+    const uint32_t x = p->x, y = p->y;
+    const size_t row_bytes = sizeof(vec2_t) * size_t(x);
+    uint32_t max_rows = 0;
+    for (uint32_t k = 0; k < k2dRowChunks; ++k)
+        max_rows = std::max<uint32_t>(max_rows, uint32_t(chunk_start(k + 1, k2dRowChunks, y) -
+                                                         chunk_start(k, k2dRowChunks, y)));
+    const size_t wrow = workspace_bytes(Px, max_rows);
+    const size_t need = r256(row_bytes * y) + r256(wrow) + columns_bytes(Py, x, y);
+    Carve cv;
+    cv.base = static_cast<char*>(g->workspace(need));
+    cv.size = need;
+    if (!cv.base) return KFFT_RET_BUFFER_FAIL;
+    vec2_t* d = static_cast<vec2_t*>(cv.take(row_bytes * y));
+    void* wr = cv.take(wrow);
+    EventSet evs;
+    for (uint32_t k = 0; k < k2dRowChunks; ++k) {
+        const uint32_t r0 = uint32_t(chunk_start(k, k2dRowChunks, y));
+        const uint32_t r1 = uint32_t(chunk_start(k + 1, k2dRowChunks, y));
+        if (r1 <= r0) continue;
+        cudaMemcpyAsync(d + size_t(r0) * x, fin + size_t(r0) * x, row_bytes * (r1 - r0),
+                        cudaMemcpyHostToDevice, cs->in);
+        cudaEvent_t e = evs.get();
+        if (!e) return KFFT_RET_BUFFER_FAIL;
+        cudaEventRecord(e, cs->in);
+        cudaStreamWaitEvent(st, e, 0);
+        if (!run_cpx(Px, d + size_t(r0) * x, d + size_t(r0) * x, r1 - r0, inverse_scale(p->flags, x),
+                     wr, wrow, st))
+            return KFFT_RET_BUFFER_FAIL;
+    }
+    if (!run_columns(Py, d, x, y, inverse_scale(p->flags, y), cv, st)) return KFFT_RET_BUFFER_FAIL;
+    cudaMemcpyAsync(fout, d, row_bytes * y, cudaMemcpyDeviceToHost, st);
+    return finish(st);
+}
+
 template <typename F>
 kfft_return_t with_staging(kfft_gpu_plan* g, size_t work, const void* const* ins,
                            const size_t* in_bytes, int nin, void* out, size_t out_bytes, F&& body) {
@@ -1157,6 +1214,9 @@ KFFT_API kfft_return_t kfft_eval2_cpx(kfft_plan_c2d* cfg, const kfft_cpx* fin, k
     if (cfg->nfft == 0) return KFFT_RET_SUCCESS;
     kfft_gpu_plan* g = cfg->plan_x->gpu;
     const size_t bytes = sizeof(vec2_t) * size_t(cfg->nfft);
+    if (c2d_pipelines(cfg, fin, fout))
+        return c2d_host_pipelined(cfg, reinterpret_cast<const vec2_t*>(fin),
+                                  reinterpret_cast<vec2_t*>(fout), g);
     const void* ins[1] = {fin};
     return with_staging(g, c2d_bytes(cfg), ins, &bytes, 1, fout, bytes,
                         [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {

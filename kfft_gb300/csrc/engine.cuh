@@ -194,6 +194,7 @@ struct PlanVariant {
     uint32_t lanes_mul = 1;      // multiplier on the default lanes of multi-pass tiles
     uint32_t single_div = 1;     // divisor on the default lanes of single-pass tiles
     uint32_t single_cap = 4096;  // longest length run as one fused pass
+    uint32_t tile_cap = kRegTile;  // most points per register tile
     bool reverse = false;        // multi-pass splits run longest pass last
     bool no_rader = false;       // primes through Bluestein even where Rader applies
     bool no_fused = false;       // shared-memory ping-pong tiles only

@@ -7,7 +7,10 @@
 
 namespace kfft {
 
-__global__ void __launch_bounds__(kPassThreads, KFFT_REG_MINBLOCKS) k_persistent(
+#ifndef KFFT_QUEUE_MINBLOCKS
+#define KFFT_QUEUE_MINBLOCKS KFFT_REG_MINBLOCKS
+#endif
+__global__ void __launch_bounds__(kPassThreads, KFFT_QUEUE_MINBLOCKS) k_persistent(
     const PassDesc* __restrict__ descs, const PassExtra* __restrict__ extras,
     const int32_t* __restrict__ deps, const QueueItem* __restrict__ items, uint32_t nitems,
     uint32_t* head, uint32_t* done, uint32_t* error, uint32_t max_polls) {

@@ -131,8 +131,8 @@ constexpr uint32_t kRegLanes = 4;
 
 // true when a tile of C lanes of length R fits the fused-I/O kernel: every
 // inner radix <= 16 and at most kRegTile points per tile
-static bool reg_tile_fits(uint32_t R, uint32_t C) {
-    if (C < 1 || uint64_t(C) * R > kRegTile) return false;
+static bool reg_tile_fits(uint32_t R, uint32_t C, uint32_t cap = kRegTile) {
+    if (C < 1 || uint64_t(C) * R > std::min(cap, kRegTile)) return false;
     if (R == 1) return true;  // a length-1 pass is a copy
     std::vector<uint8_t> rad = inner_radices(R);
     if (rad.empty() || rad.size() > size_t(kMaxInnerRadices)) return false;
@@ -188,7 +188,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     for (uint32_t f : prime_factors(N)) small_radices = small_radices && f <= 13;
     const PlanVariant& V = P->var;
     if (V.no_fused) small_radices = false;
-    if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1)) {
+    if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1, V.tile_cap)) {
         Rs.push_back(N);
     } else if (small_radices) {
 #if defined(KFFT_HALF_SCALAR)
@@ -202,7 +202,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
             if (rmax > V.rmax) continue;
             std::vector<uint32_t> cand = split_passes(N, rmax);
             bool ok = !cand.empty();
-            for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R));
+            for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R), V.tile_cap);
             if (ok) Rs = cand;
         }
     }
@@ -518,7 +518,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         bool radix_ok = (!s.radices.empty() || s.R == 1) && !P.var.no_fused;
         for (uint8_t r : s.radices) radix_ok = radix_ok && r <= 16;
         for (uint32_t c = C; radix_ok && c >= 1; --c) {
-            const bool fits = reg_tile_fits(s.R, c);
+            const bool fits = reg_tile_fits(s.R, c, P.var.tile_cap);
             const bool coalesced_enough = (d.order == ORDER_J && d.lanes_j == 1) ||
                                           c >= std::min<uint32_t>(C, kRegLanes);
             if (fits && coalesced_enough) {

@@ -24,6 +24,16 @@
 
 using namespace kfft;
 
+// Register tiles of the queue kernel: most points per tile and longest pass
+// (build-time knobs for sweeps; smaller tiles need less shared memory per
+// CTA).  The queue kernel's resident CTAs per SM are KFFT_QUEUE_MINBLOCKS.
+#ifndef KFFT_QUEUE_TILE
+#define KFFT_QUEUE_TILE 4096
+#endif
+#ifndef KFFT_QUEUE_RMAX
+#define KFFT_QUEUE_RMAX KFFT_PLAN_RMAX
+#endif
+
 namespace {
 constexpr uint32_t kUnevenMaxPrime = 13;
 
@@ -307,6 +317,8 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
             const int tv = tuned_plan_variant(n, flags);
             PlanVariant var = tv >= 0 ? plan_variant(uint32_t(tv)) : PlanVariant();
             if (var.no_fused) var = PlanVariant();
+            var.tile_cap = std::min<uint32_t>(var.tile_cap, KFFT_QUEUE_TILE);
+            var.rmax = std::min<uint32_t>(var.rmax, KFFT_QUEUE_RMAX);
             FftPlan* fp = make_plan(n, sign, P->arena, st, kUnevenMaxPrime, var);
             if (!fp) return NULL;
             P->plans[n].reset(fp);

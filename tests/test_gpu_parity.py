@@ -105,6 +105,36 @@ def test_real_vs_oracle(lib, n):
     assert rel_l2(lib.irfft(X, n), O.irfft(X, n)) <= tol64(n)
 
 
+@pytest.mark.parametrize("n,batch,flags", [(1 << 14, 6, 0), (1 << 14, 3, K.FLAG_EXPAND_SCALAR),
+                                           (1 << 17, 5, K.FLAG_EXPAND_SCALAR), (1 << 20, 2, 0),
+                                           (1 << 22, 2, 0), (8192, 4, 0), (3 << 12, 2, 0)])
+def test_real_fp32_batches_vs_oracle(libf, n, batch, flags):
+    """FP32 real transforms in batches, forward (with and without EXPAND) and
+    inverse, against the oracle sequence by sequence: single-pass (8192),
+    multi-pass power-of-two (2^14 - 2^22) and mixed-radix (3 * 2^12)
+    half lengths."""
+    rng = np.random.default_rng(n + batch)
+    x = rng.uniform(-1, 1, (batch, n)).astype(np.float32)
+    X = libf.rfft(x, flags)
+    for b in range(batch):
+        assert rel_l2(X[b], O.rfft(x[b].astype(np.float64), flags)) <= TOL32, b
+    spec = np.stack([O.rfft(x[b].astype(np.float64)) for b in range(batch)]).astype(np.complex64)
+    y = libf.irfft(spec, n)
+    for b in range(batch):
+        assert rel_l2(y[b], O.irfft(spec[b].astype(np.complex128), n)) <= TOL32, b
+
+
+@pytest.mark.parametrize("n", [1 << 16, 6000])
+def test_real_conv_fp32_product_in_the_forward_store(libf, n):
+    """A real convolution multiplies the two spectra inside the second
+    operand's post-twiddle kernel instead of a separate product sweep."""
+    rng = np.random.default_rng(n)
+    a, b = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    got = libf.conv_scalar(a.astype(np.float32), b.astype(np.float32))
+    ref = O.conv_scalar(a.astype(np.float32).astype(np.float64), b.astype(np.float32).astype(np.float64))
+    assert rel_l2(got, ref) <= TOL32
+
+
 def test_real_improper_plan(lib):
     p = lib.L.kfft_config_scalar(64, K.FLAG_INVERSE, None, None)
     x = np.zeros(64)
