@@ -25,13 +25,18 @@
 using namespace kfft;
 
 // Register tiles of the queue kernel: most points per tile and longest pass
-// (build-time knobs for sweeps; smaller tiles need less shared memory per
-// CTA).  The queue kernel's resident CTAs per SM are KFFT_QUEUE_MINBLOCKS.
+// (build-time knobs; the queue kernel's resident CTAs per SM are
+// KFFT_QUEUE_MINBLOCKS).  Tiles of at most 2048 points and passes of at most
+// 512, measured on the uneven batch of 3968 sequences: FP32 at four CTAs per
+// SM 9.38 ms against 9.96 ms for 4096 / 1024 at three (4096 / 512 at four:
+// 10.37 ms; 2048 / 512 at three: 11.48 ms; 1024 / 256 at four: 14.89 ms);
+// FP64 at three CTAs per SM 84.1 ms against 100.1 ms for 4096 / 1024 at two
+// (2048 / 512 at two: 87.7 ms).
 #ifndef KFFT_QUEUE_TILE
-#define KFFT_QUEUE_TILE 4096
+#define KFFT_QUEUE_TILE 2048
 #endif
 #ifndef KFFT_QUEUE_RMAX
-#define KFFT_QUEUE_RMAX KFFT_PLAN_RMAX
+#define KFFT_QUEUE_RMAX 512
 #endif
 
 namespace {
