@@ -38,6 +38,9 @@ using namespace kfft;
 #ifndef KFFT_QUEUE_RMAX
 #define KFFT_QUEUE_RMAX 512
 #endif
+#ifndef KFFT_QUEUE_MAXINNER
+#define KFFT_QUEUE_MAXINNER 16
+#endif
 
 namespace {
 constexpr uint32_t kUnevenMaxPrime = 13;
@@ -324,6 +327,7 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
             if (var.no_fused) var = PlanVariant();
             var.tile_cap = std::min<uint32_t>(var.tile_cap, KFFT_QUEUE_TILE);
             var.rmax = std::min<uint32_t>(var.rmax, KFFT_QUEUE_RMAX);
+            var.max_inner = std::min<uint32_t>(var.max_inner, KFFT_QUEUE_MAXINNER);
             FftPlan* fp = make_plan(n, sign, P->arena, st, kUnevenMaxPrime, var);
             if (!fp) return NULL;
             P->plans[n].reset(fp);
