@@ -861,14 +861,21 @@ def main():
     ms_total = start.elapsed_time(end)
     ms, value = aggregate_over_ranks(ms_total, wl.flops_per_step(), args.steps, ws, pg, dev)
 
-    # end to end through the C ABI with pinned host buffers
-    for _ in range(2):
+    # end to end through the C ABI with pinned host buffers.  Each step is
+    # timed on its own and the line reports the median: on the shared hosts
+    # this runs on, plain pinned copies of the same buffers stall now and
+    # then for 20-130 ms (seen with torch's pinned buffers and with
+    # registered huge-page buffers alike), which one step in a short mean
+    # would carry; the mean and the slowest step are reported beside it.
+    for _ in range(max(2, min(args.warmup, 3))):
         wl.step_e2e()
-    t0 = time.perf_counter()
-    e2e_steps = max(2, min(args.steps, 5))
+    e2e_steps = max(5, min(args.steps, 10))
+    e2e_times = []
     for _ in range(e2e_steps):
+        t0 = time.perf_counter()
         wl.step_e2e()
-    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+        e2e_times.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = float(np.median(e2e_times))
     h2d, d2h = wl.e2e_bytes()
     e2e_val = ws * wl.flops_per_step() / (e2e_ms / 1e3) / 1e9
 
@@ -883,7 +890,10 @@ def main():
             "data": "synthetic",
             "config": workload_config(wl, ws, nbuf),
             "e2e": {"value": round(e2e_val, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3),
+                    "steps": e2e_steps, "stat": "median of per-step wall times",
+                    "ms_per_step_mean": round(float(np.mean(e2e_times)), 3),
+                    "ms_per_step_max": round(float(np.max(e2e_times)), 3)},
             "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary()}
     if rank == 0 and hasattr(wl, "accuracy"):
         from oracle import oracle as _oracle

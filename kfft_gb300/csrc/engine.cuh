@@ -143,7 +143,7 @@ void fill_extras(const PassDesc* d, void* extras, size_t n);
 // A dependency wait polls at most max_polls times (about 200 ns apart) before
 // it sets the error word and skips the tile; the default allows about 3 s.
 constexpr uint32_t kQueueMaxPolls = 1u << 24;
-bool launch_persistent(const PassDesc* descs, const void* extras, const int32_t* deps,
+bool launch_persistent(const PassDesc* descs, const void* extras,
                        const void* items, uint32_t nitems, uint32_t* head, uint32_t* done,
                        uint32_t* error, uint32_t smem_bytes, cudaStream_t st,
                        uint32_t max_polls = kQueueMaxPolls);
@@ -195,7 +195,6 @@ struct PlanVariant {
     uint32_t single_div = 1;     // divisor on the default lanes of single-pass tiles
     uint32_t single_cap = 4096;  // longest length run as one fused pass
     uint32_t tile_cap = kRegTile;  // most points per register tile
-    uint32_t max_inner = 16;     // largest composite inner radix of non-power-of-two tiles
     bool reverse = false;        // multi-pass splits run longest pass last
     bool no_rader = false;       // primes through Bluestein even where Rader applies
     bool no_fused = false;       // shared-memory ping-pong tiles only
@@ -309,7 +308,7 @@ inline CopyRange copy_range(size_t b0, size_t b1, size_t total, bool first, bool
 // (power-of-two) tile body of C lanes of R points run by `threads` threads:
 // the padded lane plus the skew with the fewest bank conflicts.
 uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
-                          uint32_t threads, uint32_t maxp = 16);
+                          uint32_t threads);
 PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const Layout& lin,
                         vec2_t* out, const Layout& lout, real_t scale);
 

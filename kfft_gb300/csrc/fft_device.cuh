@@ -1476,9 +1476,13 @@ __device__ __forceinline__ void tile_body_reg(const PassDesc& d, const PassExtra
 }
 
 // ---- persistent-queue helpers --------------------------------------------
+// One queue item: tile `tile` of pass `desc`, which may start once
+// done[dep] reaches `need` (the tiles of the pass it reads; dep < 0: none).
 struct QueueItem {
     uint32_t desc;
     uint32_t tile;
+    int32_t dep;
+    uint32_t need;
 };
 
 __device__ __forceinline__ uint32_t load_acquire(const uint32_t* p) {

@@ -69,16 +69,15 @@ static uint32_t smem_for(uint32_t elems) {
 // in plan_host.h), cached per (R, C, lane modes, threads)
 // ---------------------------------------------------------------------------
 uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
-                          uint32_t threads, uint32_t maxp) {
+                          uint32_t threads) {
     static std::mutex mu;
     static std::map<std::pair<uint64_t, uint32_t>, uint32_t> cache;
     const auto key = std::make_pair((uint64_t(R) << 32) | C,
-                                    uint32_t(load_lane) | (uint32_t(store_lane) << 1) |
-                                        (uint32_t(maxp >= 16) << 2) | (threads << 3));
+                                    uint32_t(load_lane) | (uint32_t(store_lane) << 1) | (threads << 2));
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    const uint32_t best = lane_stride_search(R, C, load_lane, store_lane, threads, maxp);
+    const uint32_t best = lane_stride_search(R, C, load_lane, store_lane, threads);
     cache[key] = best;
     return best;
 }
@@ -132,10 +131,10 @@ constexpr uint32_t kRegLanes = 4;
 
 // true when a tile of C lanes of length R fits the fused-I/O kernel: every
 // inner radix <= 16 and at most kRegTile points per tile
-static bool reg_tile_fits(uint32_t R, uint32_t C, uint32_t cap = kRegTile, uint32_t maxp = 16) {
+static bool reg_tile_fits(uint32_t R, uint32_t C, uint32_t cap = kRegTile) {
     if (C < 1 || uint64_t(C) * R > std::min(cap, kRegTile)) return false;
     if (R == 1) return true;  // a length-1 pass is a copy
-    std::vector<uint8_t> rad = inner_radices(R, maxp);
+    std::vector<uint8_t> rad = inner_radices(R);
     if (rad.empty() || rad.size() > size_t(kMaxInnerRadices)) return false;
     for (uint8_t r : rad)
         if (r > 16) return false;
@@ -189,7 +188,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
     for (uint32_t f : prime_factors(N)) small_radices = small_radices && f <= 13;
     const PlanVariant& V = P->var;
     if (V.no_fused) small_radices = false;
-    if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1, V.tile_cap, V.max_inner)) {
+    if (small_radices && N <= V.single_cap && reg_tile_fits(N, 1, V.tile_cap)) {
         Rs.push_back(N);
     } else if (small_radices) {
 #if defined(KFFT_HALF_SCALAR)
@@ -203,8 +202,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
             if (rmax > V.rmax) continue;
             std::vector<uint32_t> cand = split_passes(N, rmax);
             bool ok = !cand.empty();
-            for (uint32_t R : cand)
-                ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R), V.tile_cap, V.max_inner);
+            for (uint32_t R : cand) ok = ok && reg_tile_fits(R, std::min(kRegLanes, N / R), V.tile_cap);
             if (ok) Rs = cand;
         }
     }
@@ -220,7 +218,7 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
         PassSpec s;
         s.R = R;
         s.Ns = Ns;
-        s.radices = inner_radices(R, V.max_inner);
+        s.radices = inner_radices(R);
         if (s.radices.size() > size_t(kMaxInnerRadices)) return false;
         auto it = inner.find(R);
         if (it == inner.end()) {
@@ -520,7 +518,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         bool radix_ok = (!s.radices.empty() || s.R == 1) && !P.var.no_fused;
         for (uint8_t r : s.radices) radix_ok = radix_ok && r <= 16;
         for (uint32_t c = C; radix_ok && c >= 1; --c) {
-            const bool fits = reg_tile_fits(s.R, c, P.var.tile_cap, P.var.max_inner);
+            const bool fits = reg_tile_fits(s.R, c, P.var.tile_cap);
             const bool coalesced_enough = (d.order == ORDER_J && d.lanes_j == 1) ||
                                           c >= std::min<uint32_t>(C, kRegLanes);
             if (fits && coalesced_enough) {
@@ -552,7 +550,7 @@ static PassDesc make_desc(const FftPlan& P, size_t pi, const vec2_t* in, const L
         d.threads = kPassThreads;
         const uint32_t nbuf = s.radices.size() >= 3 ? 2u : (s.radices.size() == 2 ? 1u : 0u);
         d.lane_stride = spec_lane_stride(s.R, C, d.load_mode == MODE_LANE,
-                                         d.store_mode == MODE_LANE, kPassThreads, P.var.max_inner);
+                                         d.store_mode == MODE_LANE, kPassThreads);
         d.smem_bytes = nbuf * (C * d.lane_stride + 1u) * uint32_t(sizeof(vec2_t));
     } else {
         uint32_t t = (elems + 7) / 8;

@@ -59,11 +59,8 @@ inline double radix_flops_per_point(uint32_t r) {
 // (shared-memory tiles only) are stages of their own.  Every stage is a
 // shared-memory round trip and a barrier, which is what bounds a mixed-radix
 // tile: 729 = 3^6 runs as 9, 9, 9 instead of six radix-3 stages.  Radices are
-// listed largest first.  `maxp` (8 or 16) is the largest composite radix a
-// stage of a length other than a power of two may use (the primes 11 and 13
-// stay): 8 keeps a stage's butterflies at one per thread or more in tiles of
-// 2048 points over 256 threads.
-inline std::vector<uint8_t> inner_radices(uint32_t R, uint32_t maxp = 16) {
+// listed largest first.
+inline std::vector<uint8_t> inner_radices(uint32_t R) {
     std::vector<uint8_t> r;
     if (R >= 2 && (R & (R - 1)) == 0) {
         uint32_t e2 = 0;
@@ -102,7 +99,7 @@ inline std::vector<uint8_t> inner_radices(uint32_t R, uint32_t maxp = 16) {
         const uint32_t d = divs[i];
         stages[i] = UINT32_MAX;
         for (uint32_t q : kSet) {
-            if (d % q || (q > maxp && q != 11 && q != 13)) continue;  // primes stay
+            if (d % q) continue;
             const size_t j = index_of(d / q);
             if (stages[j] == UINT32_MAX) continue;
             const uint32_t s = stages[j] + 1;
@@ -240,9 +237,9 @@ inline uint32_t smem_wavefronts(const int64_t* idx) {
 // consecutive threads on consecutive lanes; the others put them on
 // consecutive butterflies of one lane.
 inline uint64_t tile_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool load_lane,
-                               bool store_lane, uint32_t threads, uint32_t maxp = 16) {
+                               bool store_lane, uint32_t threads) {
     auto padh = [](uint64_t i) { return i + i / kRowElems; };
-    const std::vector<uint8_t> rad = inner_radices(R, maxp);
+    const std::vector<uint8_t> rad = inner_radices(R);
     const size_t np = rad.size();
     uint64_t cost = 0;
     uint32_t NS = 1;
@@ -288,13 +285,13 @@ inline uint64_t tile_smem_cost(uint32_t R, uint32_t C, uint32_t stride, bool loa
 // lane-major access can all fall in the same banks (a lane of 2^k >= 16
 // points is a whole number of 128-byte rows).  Ties go to the smaller skew.
 inline uint32_t lane_stride_search(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
-                                   uint32_t threads, uint32_t maxp = 16) {
+                                   uint32_t threads) {
     const uint32_t base = R + R / kRowElems;
     uint32_t best = base;
     uint64_t best_cost = ~uint64_t(0);
-    if (C > 1 && inner_radices(R, maxp).size() > 1) {
+    if (C > 1 && inner_radices(R).size() > 1) {
         for (uint32_t skew = 0; skew < kRowElems; ++skew) {
-            const uint64_t c = tile_smem_cost(R, C, base + skew, load_lane, store_lane, threads, maxp);
+            const uint64_t c = tile_smem_cost(R, C, base + skew, load_lane, store_lane, threads);
             if (c < best_cost) {
                 best_cost = c;
                 best = base + skew;

@@ -38,17 +38,19 @@ using namespace kfft;
 #ifndef KFFT_QUEUE_RMAX
 #define KFFT_QUEUE_RMAX 512
 #endif
-#ifndef KFFT_QUEUE_MAXINNER
-#define KFFT_QUEUE_MAXINNER 16
-#endif
 
 namespace {
 constexpr uint32_t kUnevenMaxPrime = 13;
 
+// the queue kernel's item record: tile `tile` of pass `desc`, runnable once
+// done[dep] reaches `need` (dep < 0: no dependency)
 struct Item {
     uint32_t desc;
     uint32_t tile;
+    int32_t dep;
+    uint32_t need;
 };
+static_assert(sizeof(Item) == 16, "one 16-byte record per item");
 }  // namespace
 
 // One recorded work queue over a range of sequences: descriptors, items and
@@ -59,7 +61,7 @@ struct UnevenQueue {
     uint64_t p0 = 0, p1 = 0;  // their points [p0, p1)
     const void* g_in = nullptr;
     void* g_out = nullptr;
-    void* qmem = nullptr;  // descs | extras | deps | items | counters
+    void* qmem = nullptr;  // descs | extras | items | counters
     size_t qbytes = 0;
     uint32_t* counters = nullptr;  // head, error, done[ndesc]
     size_t counter_bytes = 0;
@@ -150,7 +152,9 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
     uint32_t smem = 0;
     for (uint32_t d = 0; d < nd; ++d) {
         smem = std::max(smem, all[d].smem_bytes);
-        for (uint32_t t = 0; t < all[d].tiles; ++t) items.push_back({d, t});
+        const int32_t dep = deps[d];
+        const uint32_t need = dep >= 0 ? all[dep].tiles : 0u;
+        for (uint32_t t = 0; t < all[d].tiles; ++t) items.push_back({d, t, dep, need});
     }
     // level order (dependencies first), larger tiles first within a level.
     // (Ordering groups of sequences in a diagonal wavefront instead, so that
@@ -165,11 +169,10 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
     });
     const size_t b_desc = a256(sizeof(PassDesc) * nd);
     const size_t b_extra = a256(pass_extra_bytes() * nd);
-    const size_t b_dep = a256(sizeof(int32_t) * nd);
     const size_t b_item = a256(sizeof(Item) * items.size());
     const size_t b_cnt = a256(sizeof(uint32_t) * (nd + 2));
     Q.drop();
-    Q.qbytes = b_desc + b_extra + b_dep + b_item + b_cnt;
+    Q.qbytes = b_desc + b_extra + b_item + b_cnt;
     if (cudaMalloc(&Q.qmem, Q.qbytes) != cudaSuccess) {
         cudaGetLastError();
         Q.qmem = nullptr;
@@ -179,16 +182,14 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
     char* q = static_cast<char*>(Q.qmem);
     PassDesc* d_desc = reinterpret_cast<PassDesc*>(q);
     void* d_extra = q + b_desc;
-    int32_t* d_dep = reinterpret_cast<int32_t*>(q + b_desc + b_extra);
-    Item* d_item = reinterpret_cast<Item*>(q + b_desc + b_extra + b_dep);
-    Q.counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_dep + b_item);
+    Item* d_item = reinterpret_cast<Item*>(q + b_desc + b_extra);
+    Q.counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_item);
     Q.counter_bytes = sizeof(uint32_t) * (nd + 2);
     std::vector<char> extras(pass_extra_bytes() * nd);
     fill_extras(all.data(), extras.data(), nd);
     cudaStream_t st = cudaStreamPerThread;
     cudaMemcpyAsync(d_desc, all.data(), sizeof(PassDesc) * nd, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_extra, extras.data(), extras.size(), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d_dep, deps.data(), sizeof(int32_t) * nd, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_item, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return false;
     Q.ndesc = nd;
@@ -201,7 +202,7 @@ bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) 
     if (e == cudaSuccess) {
         cudaMemsetAsync(Q.counters, 0, Q.counter_bytes, cap);
         if (Q.nitems)
-            launch_persistent(d_desc, d_extra, d_dep, d_item, Q.nitems, Q.counters,
+            launch_persistent(d_desc, d_extra, d_item, Q.nitems, Q.counters,
                               Q.counters + 2, Q.counters + 1, smem, cap);
         e = cudaStreamEndCapture(cap, &graph);
     }
@@ -327,7 +328,6 @@ KFFT_API kfft_plan_uneven* kfft_config_cpx_uneven(uint32_t count, const uint32_t
             if (var.no_fused) var = PlanVariant();
             var.tile_cap = std::min<uint32_t>(var.tile_cap, KFFT_QUEUE_TILE);
             var.rmax = std::min<uint32_t>(var.rmax, KFFT_QUEUE_RMAX);
-            var.max_inner = std::min<uint32_t>(var.max_inner, KFFT_QUEUE_MAXINNER);
             FftPlan* fp = make_plan(n, sign, P->arena, st, kUnevenMaxPrime, var);
             if (!fp) return NULL;
             P->plans[n].reset(fp);
@@ -475,11 +475,10 @@ KFFT_API int kfft_gb300_queue_selftest(uint32_t max_polls, int satisfiable) {
     if (!ensure_device()) return -1;
     const size_t b_desc = a256(2 * sizeof(PassDesc));
     const size_t b_extra = a256(2 * pass_extra_bytes());
-    const size_t b_dep = a256(2 * sizeof(int32_t));
     const size_t b_item = a256(2 * sizeof(Item));
     const size_t b_cnt = a256(4 * sizeof(uint32_t));
     void* mem = nullptr;
-    if (cudaMalloc(&mem, b_desc + b_extra + b_dep + b_item + b_cnt) != cudaSuccess) {
+    if (cudaMalloc(&mem, b_desc + b_extra + b_item + b_cnt) != cudaSuccess) {
         cudaGetLastError();
         return -1;
     }
@@ -493,22 +492,19 @@ KFFT_API int kfft_gb300_queue_selftest(uint32_t max_polls, int satisfiable) {
         x.batch = 0;
         x.threads = kPassThreads;
     }
-    const int32_t deps[2] = {-1, 0};
-    const Item items[2] = {{0, 0}, {1, 0}};
+    const Item items[2] = {{0, 0, -1, 0}, {1, 0, 0, 1}};
     const Item* first = satisfiable ? items : items + 1;
     const uint32_t nitems = satisfiable ? 2u : 1u;
     std::vector<char> extras(2 * pass_extra_bytes(), 0);
     cudaStream_t st = cudaStreamPerThread;
-    uint32_t* counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_dep + b_item);
+    uint32_t* counters = reinterpret_cast<uint32_t*>(q + b_desc + b_extra + b_item);
     cudaMemcpyAsync(q, d, sizeof(d), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(q + b_desc, extras.data(), extras.size(), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(q + b_desc + b_extra, deps, sizeof(deps), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(q + b_desc + b_extra + b_dep, first, nitems * sizeof(Item),
-                    cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(q + b_desc + b_extra, first, nitems * sizeof(Item), cudaMemcpyHostToDevice,
+                    st);
     cudaMemsetAsync(counters, 0, 4 * sizeof(uint32_t), st);
-    launch_persistent(reinterpret_cast<PassDesc*>(q), q + b_desc,
-                      reinterpret_cast<int32_t*>(q + b_desc + b_extra), q + b_desc + b_extra + b_dep,
-                      nitems, counters, counters + 2, counters + 1, 0, st, max_polls);
+    launch_persistent(reinterpret_cast<PassDesc*>(q), q + b_desc, q + b_desc + b_extra, nitems,
+                      counters, counters + 2, counters + 1, 0, st, max_polls);
     uint32_t err = 0;
     cudaMemcpyAsync(&err, counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);
