@@ -931,7 +931,8 @@ def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, devi
 # points, which the same length mix allows.
 NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.708141e9 / 37465227}
 NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.3e6, "c2c_f32_2p18x64": 216.7e6,
-                             "c2c_f32_2p20x16": 215.7e6, "c2c_f32_2p24": 215.9e6}
+                             "c2c_f32_2p20x16": 215.7e6, "c2c_f32_2p24": 215.9e6,
+                             "c2c4096": 18.7e6}
 
 
 def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_step=None,
@@ -955,9 +956,12 @@ def dominant_kernel_roofline(wl, ms_step, lib, peak, peak_kind, launches_per_ste
         achieved = per_launch / (dur / 1e3) / 1e9
         per_transform = wl.algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9
         traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(workload)
+        generic = wl.precision == "double" or getattr(wl, "tc", False)
+        kernel = ("k_pass_reg (one launch per pass)" if generic else
+                  "k_pass_bulk / k_pass_pipe / k_pass_pipe_wide (one launch per pass)")
         return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "k_pass_bulk / k_pass_pipe / k_pass_pipe_wide (one launch per pass)",
+                "kernel": kernel,
                 "launches_per_step": n, "launch_ms": round(dur, 4),
                 "per_transform_gbs": round(per_transform, 1)}
     # the uneven batch: one k_persistent launch runs every pass of every sequence
