@@ -514,6 +514,17 @@ struct PassExtra {
 
 PassExtra make_extra(const PassDesc& d);
 
+// The outer twiddle W_N^e of a pass (e < N): the product of the two-level
+// table's entries, or, in an FP64 plan with tw_shift 0, one entry of the full
+// table (one complex product fewer on the FP64 pipe).
+__device__ __forceinline__ vec2_t outer_w(const PassDesc& d, uint32_t e) {
+#if !defined(KFFT_HALF_SCALAR)
+    if (d.tw_shift == 0) return __ldg(&d.tw_hi[e]);
+#endif
+    const uint32_t mask = (1u << d.tw_shift) - 1u;
+    return cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
+}
+
 // One tile of one pass: C lanes of the length-R sub-FFT, shared-memory staged.
 template <bool INV, bool BIG>
 __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x, uint32_t tile,
@@ -563,12 +574,8 @@ __device__ __forceinline__ void tile_body(const PassDesc& d, const PassExtra& x,
             }
         }
         if (d.Ns > 1) {
-            const uint32_t mask = (1u << d.tw_shift) - 1u;
 #pragma unroll
-            for (int u = 0; u < kLoadUnroll; ++u) {
-                const vec2_t w = cmul(__ldg(&d.tw_hi[twe[u] >> d.tw_shift]), __ldg(&d.tw_lo[twe[u] & mask]));
-                v[u] = cmul(v[u], w);
-            }
+            for (int u = 0; u < kLoadUnroll; ++u) v[u] = cmul(v[u], outer_w(d, twe[u]));
         }
 #pragma unroll
         for (int u = 0; u < kLoadUnroll; ++u)
@@ -695,16 +702,13 @@ __device__ __forceinline__ void outer_twiddle(const PassDesc& d, uint32_t j, uin
     if (d.Ns > 1) {
         const uint32_t kq = fdiv(j, d.div_Ns);
         const uint32_t k = j - kq * d.Ns;
-        const uint32_t mask = (1u << d.tw_shift) - 1u;
         const uint32_t e0 = uint32_t(uint64_t(jj) * k * d.tw_mul);
         const uint32_t es = uint32_t(uint64_t(m) * k * d.tw_mul);
 #if defined(KFFT_HALF_SCALAR)
         if constexpr (P >= 4) {
             // FP32: W^(e0 + q es) from the base W^(e0) and the anchors W^(2^b es):
             // ten table loads per butterfly instead of 2P (the L1 bottleneck)
-            auto tw2 = [&](uint32_t e) {
-                return cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
-            };
+            auto tw2 = [&](uint32_t e) { return outer_w(d, e); };
             const vec2_t w0 = tw2(e0);
             vec2_t a[4];
 #pragma unroll
@@ -727,10 +731,7 @@ __device__ __forceinline__ void outer_twiddle(const PassDesc& d, uint32_t j, uin
             vec2_t w[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (g + u < P) {
-                    const uint32_t e = e0 + uint32_t(g + u) * es;  // < N, no wrap
-                    w[u] = cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
-                }
+                if (g + u < P) w[u] = outer_w(d, e0 + uint32_t(g + u) * es);  // < N, no wrap
 #pragma unroll
             for (int u = 0; u < 4; ++u)
                 if (g + u < P) v[g + u] = cmul(v[g + u], w[u]);

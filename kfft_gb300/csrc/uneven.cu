@@ -266,10 +266,10 @@ kfft_return_t launch(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2
 // of one group overlap the transform of its neighbours.
 // Host-buffer calls split the batch into at most KFFT_UNEVEN_GROUPS groups
 // of at least 2^KFFT_UNEVEN_GROUP_LOG2 points (measured on the default uneven
-// batch: 8 groups 18.9 ms per e2e step, 16 18.2, 32 17.9, 64 30.3, before the
-// copies were aligned; 16 keeps the recorded graphs few).
+// batch with aligned copies: 12 groups 14.97 ms per e2e call, 16 14.62, 24
+// 14.31, 32 14.35; before the copies were aligned 64 groups took 30.3 ms).
 #ifndef KFFT_UNEVEN_GROUPS
-#define KFFT_UNEVEN_GROUPS 16
+#define KFFT_UNEVEN_GROUPS 24
 #endif
 #ifndef KFFT_UNEVEN_GROUP_LOG2
 #define KFFT_UNEVEN_GROUP_LOG2 23
