@@ -515,12 +515,8 @@ struct PassExtra {
 PassExtra make_extra(const PassDesc& d);
 
 // The outer twiddle W_N^e of a pass (e < N): the product of the two-level
-// table's entries, or, in an FP64 plan with tw_shift 0, one entry of the full
-// table (one complex product fewer on the FP64 pipe).
+// table's entries W_N^(e >> tw_shift << tw_shift) and W_N^(e mod 2^tw_shift).
 __device__ __forceinline__ vec2_t outer_w(const PassDesc& d, uint32_t e) {
-#if !defined(KFFT_HALF_SCALAR)
-    if (d.tw_shift == 0) return __ldg(&d.tw_hi[e]);
-#endif
     const uint32_t mask = (1u << d.tw_shift) - 1u;
     return cmul(__ldg(&d.tw_hi[e >> d.tw_shift]), __ldg(&d.tw_lo[e & mask]));
 }

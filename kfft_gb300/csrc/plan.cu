@@ -141,11 +141,6 @@ static bool reg_tile_fits(uint32_t R, uint32_t C, uint32_t cap = kRegTile) {
     return true;
 }
 
-// FP64 outer twiddles from one full table instead of two (build-time knob)
-#ifndef KFFT_F64_FULL_TWIDDLE
-#define KFFT_F64_FULL_TWIDDLE 0
-#endif
-
 // ---------------------------------------------------------------------------
 // device arena
 // ---------------------------------------------------------------------------
@@ -236,19 +231,6 @@ static bool build_direct(FftPlan* P, DeviceArena& arena, cudaStream_t st) {
         P->passes.push_back(s);
         Ns *= R;
     }
-#if !defined(KFFT_HALF_SCALAR) && KFFT_F64_FULL_TWIDDLE
-    // FP64 plans of up to 2^22 points: one full table of the outer twiddles
-    // (tw_shift 0), which saves a complex product per point on the FP64 pipe
-    if (P->passes.size() > 1 && N <= (1u << 22)) {
-        vec2_t* full = static_cast<vec2_t*>(arena.alloc(sizeof(vec2_t) * N));
-        if (!full) return false;
-        gen_twiddles(full, N, 1, N, P->sign, st);
-        P->tw_lo = full;
-        P->tw_hi = full;
-        P->tw_shift = 0;
-        return true;
-    }
-#endif
     if (P->passes.size() > 1) {
         uint32_t bits = 0;
         while ((uint64_t(1) << bits) < N) ++bits;
