@@ -21,9 +21,13 @@ def tol64(n):
 TOL32 = 1e-6
 
 # The opt-in tensor-core radix-16 stages (KFFT_FLAG_TENSOR_CORES) split the
-# FP32 data and the DFT matrix into two FP16 terms each, about 22 significand
-# bits against FP32's 24, so they do not meet TOL32 on every input: measured
-# 1.05e-6 at 2^24, 1.23e-6 on the high-dynamic-range input at 64 x 2^18 and
-# 1.96e-6 on the Rader prime 65537 (7e-7 and below on the smaller sizes).
-# Their tests hold this looser bound and say so; the default path meets TOL32.
-TOL32_TC = 2.5e-6
+# FP32 data and the DFT matrix into two FP16 terms each (about 22 significand
+# bits against FP32's 24) and sum the small cross products before the large
+# one; they are held to the same bound (measured 6.3e-7 at 2^24, 5.0e-7 on
+# the high-dynamic-range input at 64 x 2^18) ...
+TOL32_TC = TOL32
+# ... except inside a Rader or Bluestein convolution, whose forward and
+# inverse sub-transforms both carry the split's error: 1.14e-6 on the prime
+# 65537 (the reference's own float build reaches about 1.2e-6 on Rader
+# primes with no tensor cores at all).
+TOL32_TC_CONV = 1.5e-6

@@ -313,8 +313,7 @@ def test_uneven_workload_subset(precision):
 def test_tensor_core_radix16_path(libf, n, batch):
     """FP32 build with KFFT_FLAG_TENSOR_CORES: FP16 split hi+lo radix-16
     stages, held to the plain FP32 bound at these sizes (up to 2^20; the
-    larger benchmark sizes, where the split's 22 bits miss it, are in
-    test_gpu_config_sizes.py)."""
+    larger benchmark sizes are in test_gpu_config_sizes.py)."""
     rng = np.random.default_rng(n)
     x = cx(rng, batch, n).astype(np.complex64)
     ref = O.fft_cpx(x.astype(np.complex128))

@@ -1,9 +1,9 @@
 """Plan variants, the tuning table and the learned cost model on the GPU.
 
 * Every plan variant computes the same transform: parity with the FP64 oracle
-  (FP64 build: rel-L2 <= 1e-13*log2 N; FP32 build: 1e-6, and 2.5e-6 for
-  the opt-in tensor-core variant, whose two-term FP16 split misses 1e-6 on
-  some lengths).
+  (FP64 build: rel-L2 <= 1e-13*log2 N; FP32 build: 1e-6, also for the
+  opt-in tensor-core variant except inside Rader and Bluestein plans, where
+  its two-term FP16 split is held to 1.5e-6).
 * kfft_tune_set steers plain kfft_config_cpx calls.
 * The MLP kernels: forward, loss and gradient against the FP64 numpy
   restatement (FP32 kernels: relative error <= 1e-4), one Adam step against
@@ -21,7 +21,7 @@ import kfft_gb300 as K
 from kfft_gb300 import tuner as T
 from oracle import mlp_ref
 from oracle import oracle as O
-from tests.helpers import TOL32, TOL32_TC, rel_l2, tol64
+from tests.helpers import TOL32, TOL32_TC, TOL32_TC_CONV, rel_l2, tol64
 
 pytestmark = pytest.mark.gpu
 
@@ -67,8 +67,10 @@ def test_every_variant_matches_oracle_fp32(libf, n):
     for v in range(nvar):
         tc = v == nvar - 1
         y, desc = _eval_variant(libf, n, v, x, K.FLAG_TENSOR_CORES if tc else 0)
-        # the tensor-core variant is held to its own documented bound
-        assert rel_l2(y[0], ref) <= (TOL32_TC if tc else TOL32), (n, v, desc)
+        # the tensor-core variant is held to its own documented bounds
+        conv = "rader" in desc or "bluestein" in desc
+        tol = (TOL32_TC_CONV if conv else TOL32_TC) if tc else TOL32
+        assert rel_l2(y[0], ref) <= tol, (n, v, desc)
 
 
 def test_tensor_core_variant_needs_the_flag(libf, lib):
