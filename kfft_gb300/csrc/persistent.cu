@@ -24,6 +24,14 @@ namespace kfft {
 #define KFFT_QUEUE_MINBLOCKS 3
 #endif
 #endif
+// threads per CTA of the queue kernel (its tile bodies stride over the
+// CTA's threads, whatever their number).  Uneven FP32 batch: 256 threads,
+// 2048-point tiles, 4 CTAs per SM 8.85 ms; 128 threads, 1024-point tiles,
+// 256-point passes, 8 CTAs 9.05 ms (6 CTAs 10.17); 512 threads,
+// 4096-point tiles, 2 CTAs 9.47 ms with 1024-point passes, 10.10 with 512.
+#ifndef KFFT_QUEUE_THREADS
+#define KFFT_QUEUE_THREADS 256
+#endif
 // 1: each CTA claims its items two ahead and copies the next item's record
 // into shared memory while the current one runs; 0: one claim ahead, the
 // record read when its turn comes (uneven FP32 batch: 8.93 against 9.13 ms;
@@ -74,7 +82,7 @@ __device__ __forceinline__ void run_item(const PassDesc& d, const PassExtra& x, 
     else tile_body_reg<false, true, false>(d, x, tile, buf);
 }
 
-__global__ void __launch_bounds__(kPassThreads, KFFT_QUEUE_MINBLOCKS) k_persistent(
+__global__ void __launch_bounds__(KFFT_QUEUE_THREADS, KFFT_QUEUE_MINBLOCKS) k_persistent(
     const PassDesc* __restrict__ descs, const PassExtra* __restrict__ extras,
     const QueueItem* __restrict__ items, uint32_t nitems, uint32_t* head, uint32_t* done,
     uint32_t* error, uint32_t max_polls) {
@@ -184,13 +192,13 @@ bool launch_persistent(const PassDesc* descs, const void* extras,
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_persistent,
-                                                          kPassThreads, configured_smem);
+                                                          KFFT_QUEUE_THREADS, configured_smem);
             if (blocks_per_sm < 1) blocks_per_sm = 1;
         }
         grid = uint32_t(sms * blocks_per_sm);
     }
     if (grid > nitems) grid = nitems ? nitems : 1;
-    k_persistent<<<grid, kPassThreads, smem_bytes, st>>>(
+    k_persistent<<<grid, KFFT_QUEUE_THREADS, smem_bytes, st>>>(
         descs, static_cast<const PassExtra*>(extras), static_cast<const QueueItem*>(items),
         nitems, head, done, error, max_polls);
     note_cuda_error(cudaGetLastError());
