@@ -1308,6 +1308,67 @@ kfft_gpu_plan* s2d_handle(const kfft_plan_s2d* p) {
         return reinterpret_cast<const kfft_plan_cpx*>(p->plan_x)->gpu;
     return reinterpret_cast<const kfft_plan_cpx*>(p->plan_y)->gpu;
 }
+
+// The real conv2d plan as built here: the reference's struct (the base, so
+// the caller's kfft_plan_s2cnv* is this object) and, for an even x, the two
+// plans of the half-spectrum inverse.
+struct S2cnvPlan : kfft_plan_s2cnv {
+    kfft_plan_cpx* cols_inv;   // y-point complex inverse over the x/2 + 1 columns
+    kfft_plan_sclr* rows_inv;  // x-point real inverse of each row from x/2 + 1 bins
+};
+
+bool s2cnv_half_spectrum(uint32_t x, uint32_t y) { return x >= 2 && x % 2 == 0 && y >= 1; }
+
+// Circular 2D convolution of two real y-by-x arrays through half spectra (x
+// even).  The rows' real transforms keep bins 0..x/2 (hx = x/2 + 1 a row),
+// the column transforms run over those hx columns only, the spectrum product
+// is fused into the second operand's last column pass, and the inverse runs
+// the complex columns, then each row's real inverse from its hx bins: about
+// half the column work and half the spectrum traffic of the expanded spectra
+// (ext/conv2d/kfft_scalar_conv.c computes full spectra).  The result is the
+// same: the factor 2 of an even-length real inverse (kfft_scalar.c:218-242),
+// which the reference picks up in its columns when y is even, comes from the
+// rows here, so an odd y takes a factor 1/2 in the column scale.
+kfft_return_t s2cnv_half_eval(const S2cnvPlan* Q, const kfft_scalar* fin_A,
+                              const kfft_scalar* fin_B, kfft_scalar* fout) {
+    const kfft_plan_s2cnv* plan = Q;
+    const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(plan->plan_fwd->plan_x);
+    const kfft_plan_cpx* cy = reinterpret_cast<const kfft_plan_cpx*>(plan->plan_fwd->plan_y);
+    const uint32_t x = plan->x, y = plan->y, hx = x / 2 + 1;
+    const size_t nh = size_t(hx) * y;
+    const size_t rb = sizeof(real_t) * size_t(plan->nfft), hb = sizeof(vec2_t) * nh;
+    const size_t fwd_work = real_forward_bytes(rx, y) + columns_bytes(*gp(cy), hx, y);
+    const size_t inv_work =
+        columns_bytes(*gp(Q->cols_inv), hx, y) + real_inverse_bytes(Q->rows_inv, y);
+    const size_t work = 2 * r256(hb) + std::max(fwd_work, inv_work);
+    real_t cscale = inverse_scale(Q->cols_inv->flags, y);
+    if ((y % 2) && !(Q->cols_inv->flags & KFFT_FLAG_DISABLE_NORM)) cscale *= real_t(0.5);
+    const void* ins[2] = {fin_A, fin_B};
+    const size_t ibs[2] = {rb, rb};
+    return with_staging(cy->gpu, work, ins, ibs, 2, fout, rb,
+                        [&](const void* const* di, void* dout, Carve& cv, cudaStream_t st) {
+                            vec2_t* fa = static_cast<vec2_t*>(cv.take(hb));
+                            vec2_t* fb = static_cast<vec2_t*>(cv.take(hb));
+                            if (!fa || !fb) return false;
+                            const size_t mark = cv.used;
+                            const real_t* a = static_cast<const real_t*>(di[0]);
+                            const real_t* b = static_cast<const real_t*>(di[1]);
+                            if (!real_forward_dev(rx, a, fa, y, hx, 0, cv, st)) return false;
+                            if (!run_columns(*gp(cy), fa, hx, y, real_t(1), cv, st)) return false;
+                            cv.used = mark;
+                            if (!real_forward_dev(rx, b, fb, y, hx, 0, cv, st)) return false;
+                            bool fused = false;
+                            Product pr;
+                            pr.mul = fa;
+                            pr.fused = &fused;
+                            if (!run_columns(*gp(cy), fb, hx, y, real_t(1), cv, st, pr)) return false;
+                            cv.used = mark;
+                            if (!fused) launch_hadamard(fb, fa, nh, st);
+                            if (!run_columns(*gp(Q->cols_inv), fb, hx, y, cscale, cv, st)) return false;
+                            return real_inverse_dev(Q->rows_inv, fb, hx, static_cast<real_t*>(dout), y,
+                                                    cv, st);
+                        });
+}
 }  // namespace
 
 extern "C" {
@@ -1513,21 +1574,33 @@ KFFT_API kfft_return_t kfft_eval2_conv_cpx(kfft_plan_c2cnv* plan, const kfft_cpx
 KFFT_API kfft_plan_s2cnv* kfft_config2_conv_scalar(const uint32_t x, const uint32_t y,
                                                    const uint32_t flags, kfft_pool_t* A,
                                                    size_t* lenmem) {
-    size_t fwd = 0, inv = 0;
-    kfft_config2_scalar(x, y, KFFT_CHECK_FLAGS_CCNV(flags), NULL, &fwd);
-    kfft_config2_scalar(x, y, KFFT_CHECK_FLAGS_CCNV(flags) | KFFT_FLAG_INVERSE, NULL, &inv);
-    size_t memneed = sizeof(kfft_plan_s2cnv) + fwd + inv + 16;
+    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
+    size_t fwd = 0, inv = 0, cinv = 0, rinv = 0;
+    kfft_config2_scalar(x, y, cf, NULL, &fwd);
+    kfft_config2_scalar(x, y, cf | KFFT_FLAG_INVERSE, NULL, &inv);
+    const bool half = s2cnv_half_spectrum(x, y);
+    if (half) {
+        kfft_config_cpx(y, cf | KFFT_FLAG_INVERSE, NULL, &cinv);
+        kfft_config_scalar(x, cf | KFFT_FLAG_INVERSE, NULL, &rinv);
+    }
+    size_t memneed = sizeof(S2cnvPlan) + fwd + inv + cinv + rinv + 32;
     kfft_pool_t* mm = nullptr;
-    kfft_plan_s2cnv* P = plan_prepare<kfft_plan_s2cnv>(flags, memneed, A, lenmem, &mm);
-    if (!P) return NULL;
+    S2cnvPlan* Q = plan_prepare<S2cnvPlan>(flags, memneed, A, lenmem, &mm);
+    if (!Q) return NULL;
+    kfft_plan_s2cnv* P = Q;
     P->nfft = x * y;
     P->x = x;
     P->y = y;
     P->flags = flags;
-    const uint32_t cf = KFFT_CHECK_FLAGS_CCNV(flags);
     P->plan_fwd = kfft_config2_scalar(x, y, cf, mm, NULL);
     P->plan_inv = kfft_config2_scalar(x, y, cf | KFFT_FLAG_INVERSE, mm, NULL);
-    if (!P->plan_fwd || !P->plan_inv) {
+    bool ok = P->plan_fwd && P->plan_inv;
+    if (ok && half) {
+        Q->cols_inv = kfft_config_cpx(y, cf | KFFT_FLAG_INVERSE, mm, NULL);
+        Q->rows_inv = kfft_config_scalar(x, cf | KFFT_FLAG_INVERSE, mm, NULL);
+        ok = Q->cols_inv && Q->rows_inv;
+    }
+    if (!ok) {
         plan_terminate(P, A);
         return NULL;
     }
@@ -1538,6 +1611,8 @@ KFFT_API kfft_return_t kfft_eval2_conv_scalar(kfft_plan_s2cnv* plan, const kfft_
                                               const kfft_scalar* fin_B, kfft_scalar* fout) {
     if (!plan || !fin_A || !fin_B || !fout) return KFFT_RET_BADARGUMENTS;
     if (plan->nfft == 0) return KFFT_RET_SUCCESS;
+    const S2cnvPlan* Q = static_cast<const S2cnvPlan*>(plan);
+    if (Q->cols_inv && Q->rows_inv) return s2cnv_half_eval(Q, fin_A, fin_B, fout);
     kfft_gpu_plan* g = s2d_handle(plan->plan_fwd);
     const size_t n = plan->nfft;
     const size_t rb = sizeof(real_t) * n, sb = sizeof(vec2_t) * n;

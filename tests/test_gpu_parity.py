@@ -184,13 +184,26 @@ def test_conv_fixtures(lib, golden):
         assert rel_l2(lib.conv_scalar(a.real, b.real), golden[f"sc_out_{n}"]) <= tol64(n), n
 
 
-@pytest.mark.parametrize("shape", [(12, 30), (64, 64), (100, 33)])
+@pytest.mark.parametrize("shape", [(12, 30), (64, 64), (100, 33), (33, 100), (31, 2), (1, 8)])
 def test_conv2_vs_oracle(lib, shape):
     rng = np.random.default_rng(11)
     a, b = cx(rng, *shape), cx(rng, *shape)
     t = tol64(shape[0] * shape[1])
     assert rel_l2(lib.conv2_cpx(a, b), O.conv2_cpx(a, b)) <= t
     assert rel_l2(lib.conv2_scalar(a.real, b.real), O.conv2_scalar(a.real, b.real)) <= t
+
+
+@pytest.mark.parametrize("shape", [(12, 30), (33, 100), (100, 33)])
+def test_conv2_scalar_unnormalised(lib, libf, shape):
+    """Real conv2d without normalisation (KFFT_FLAG_DISABLE_NORM): an even
+    row length runs through half spectra, an odd one through the expanded
+    spectra; both must give the reference's unnormalised sums."""
+    rng = np.random.default_rng(12)
+    a, b = rng.uniform(-1, 1, shape), rng.uniform(-1, 1, shape)
+    ref = O.conv2_scalar(a, b, O.FLAG_DISABLE_NORM)
+    t = tol64(shape[0] * shape[1])
+    assert rel_l2(lib.conv2_scalar(a, b, K.FLAG_DISABLE_NORM), ref) <= t
+    assert rel_l2(libf.conv2_scalar(a, b, K.FLAG_DISABLE_NORM), ref) <= TOL32
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 7, 64, 330, 4096, 4099, 8191, 1 << 16])
