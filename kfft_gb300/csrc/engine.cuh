@@ -134,10 +134,11 @@ void scale_table(vec2_t* t, uint32_t count, double s, cudaStream_t st);
 // ---- kernels run by the executor ------------------------------------------
 void launch_pass(const PassDesc& d, cudaStream_t st);
 // Persistent work-queue execution of many pass chains in one launch: `items`
-// lists (desc, tile) pairs ordered by dependency level; deps[d] is the pass
-// that must finish before any tile of pass d starts (-1: none).  A bounded wait
-// that gives up sets *error instead of hanging.  Every pass must be a
-// register-resident tile (PassDesc::regmode).
+// lists 16-byte (desc, tile, dep, need) records ordered by dependency level;
+// a tile of pass desc starts once done[dep] reaches need, the tile count of
+// pass dep (dep -1: no dependency).  A bounded wait that gives up sets *error
+// instead of hanging.  Every pass must be a register-resident tile
+// (PassDesc::regmode).
 size_t pass_extra_bytes();
 void fill_extras(const PassDesc* d, void* extras, size_t n);
 // A dependency wait polls at most max_polls times (about 200 ns apart) before

@@ -117,8 +117,9 @@ real_t scale_for(uint32_t flags, uint32_t n) {
 
 size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Builds the pass chain of every sequence of Q's range, the dependency table
-// and the level-ordered queue, uploads them and records the graph.
+// Builds the pass chain of every sequence of Q's range and the level-ordered
+// queue of item records (each with the pass it waits for), uploads them and
+// records the graph.
 bool record(kfft_plan_uneven* P, UnevenQueue& Q, const vec2_t* in, vec2_t* out) {
     std::vector<PassDesc> all;
     std::vector<int32_t> deps;
