@@ -297,6 +297,12 @@ PlanVariant plan_variant(uint32_t index) {
     return v;
 }
 
+// 1: a Bluestein plan sizes its convolution for the pass limits of its own
+// variant (the uneven batch's 2048-point tiles and 512-point passes)
+#ifndef KFFT_BLUESTEIN_PLAN_AWARE
+#define KFFT_BLUESTEIN_PLAN_AWARE 1
+#endif
+
 FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
                    uint32_t max_prime, const PlanVariant& var) {
     FftPlan* P = new FftPlan();
@@ -361,7 +367,13 @@ FftPlan* make_plan(uint32_t N, int sign, DeviceArena& arena, cudaStream_t st,
     }
     // ---- Bluestein: X_k = c_k sum_n (x_n c_n) conj(c_{k-n}) --------------------
     P->method = METHOD_BLUESTEIN;
+#if KFFT_BLUESTEIN_PLAN_AWARE
+    const uint32_t b_rmax = std::min(var.rmax, kMultiRmax);
+    const uint32_t b_single = std::min(std::min(var.tile_cap, var.single_cap), kRegTile);
+    uint64_t M = bluestein_length(2 * uint64_t(N) - 1, b_rmax, b_single);
+#else
     uint64_t M = bluestein_length(2 * uint64_t(N) - 1);
+#endif
     if (M > 0xFFFFFFFFull) {
         delete P;
         return nullptr;

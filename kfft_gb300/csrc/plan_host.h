@@ -170,11 +170,14 @@ inline std::vector<uint32_t> split_passes(uint32_t N, uint32_t rmax) {
 // factors).  A pass is one HBM round trip, and radix-3/5/7 stages cost about
 // 30% more per point than radix-2/4/8/16 ones on this kernel; the nearest
 // 7-smooth length is often odd-heavy or one pass deeper than a power-of-two
-// one slightly above it.
+// one slightly above it.  `rmax` and `single` are the plan's longest pass of
+// a multi-pass split and longest one-pass length (the uneven batch's queue
+// plans use 512 and 2048).
 #ifndef KFFT_BLUESTEIN_ODD_COST
 #define KFFT_BLUESTEIN_ODD_COST 0.15
 #endif
-inline uint64_t bluestein_length(uint64_t m) {
+inline uint64_t bluestein_length(uint64_t m, uint32_t rmax = kMultiRmax,
+                                 uint32_t single = kRegTile) {
     uint64_t best = next_smooth(m);
     double best_cost = -1.0;
     for (uint64_t a = 1; a <= 2 * m; a *= 2)
@@ -189,8 +192,8 @@ inline uint64_t bluestein_length(uint64_t m) {
                             r /= q;
                             ++odd;
                         }
-                    const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), kMultiRmax).size());
-                    const double cost = double(d) * double(d <= kRegTile ? 1 : passes) *
+                    const size_t passes = std::max<size_t>(1, split_passes(uint32_t(d), rmax).size());
+                    const double cost = double(d) * double(d <= single ? 1 : passes) *
                                         (1.0 + KFFT_BLUESTEIN_ODD_COST * odd);
                     if (best_cost < 0 || cost < best_cost) {
                         best_cost = cost;

@@ -27,8 +27,12 @@ int main() {
                     (unsigned long long)kfft::tile_smem_cost(R, C, s, ll, sl, T),
                     (unsigned long long)kfft::tile_smem_cost(R, C, base, ll, sl, T));
     }
-    for (uint32_t n : {5u, 17u, 127u, 1009u, 4099u, 65521u, 104729u, 700523u, 999983u})
+    for (uint32_t n : {5u, 17u, 127u, 1009u, 4099u, 65521u, 104729u, 700523u, 999983u}) {
         std::printf("bluestein %u %llu\n", n, (unsigned long long)kfft::bluestein_length(2ull * n - 1));
+        // the pass limits of the uneven batch's queue plans
+        std::printf("bluestein_q %u %llu\n", n,
+                    (unsigned long long)kfft::bluestein_length(2ull * n - 1, 512, 2048));
+    }
     for (uint32_t n : {240240u, 1000000u, 729000u, 1081080u, 4096u * 243u})
         for (uint32_t rmax : {1024u, 512u, 256u}) {
             std::printf("balanced %u %u", n, rmax);

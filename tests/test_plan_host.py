@@ -210,7 +210,7 @@ def balanced(n, rmax):
     return []
 
 
-def bluestein(m):
+def bluestein(m, rmax=1024, single=4096):
     best, best_cost = None, None
     a = 1
     while a <= 2 * m:
@@ -226,7 +226,7 @@ def bluestein(m):
                             while r % q == 0:
                                 r //= q
                                 odd += 1
-                        passes = 1 if d <= 4096 else max(1, len(balanced(d, 1024)))
+                        passes = 1 if d <= single else max(1, len(balanced(d, rmax)))
                         cost = d * passes * (1.0 + 0.15 * odd)
                         if best_cost is None or cost < best_cost:
                             best, best_cost = d, cost
@@ -252,6 +252,17 @@ def test_bluestein_lengths_match_restatement(printed):
         assert m == bluestein(2 * n - 1), (n, m)
         assert m >= 2 * n - 1
     assert got[999983] == 1 << 21  # over the nearest 7-smooth length, 2,000,000
+
+
+def test_bluestein_lengths_for_queue_plans(printed):
+    """The uneven batch's plans (2048-point tiles, 512-point passes) size
+    their Bluestein convolutions for those limits."""
+    rows = [r for r in printed if r[0] == "bluestein_q"]
+    assert len(rows) == 9
+    for r in rows:
+        n, m = int(r[1]), int(r[2])
+        assert m == bluestein(2 * n - 1, 512, 2048), (n, m)
+        assert m >= 2 * n - 1
 
 
 def test_inner_radix_schedules_match_restatement(printed):
