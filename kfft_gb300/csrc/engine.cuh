@@ -158,6 +158,11 @@ void launch_real_post(const vec2_t* z, vec2_t* out, const vec2_t* st_tab, uint32
 // Even-N real inverse pre-processing (kfft_scalar.c:218-242).
 void launch_real_pre(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
                      uint32_t batch, uint64_t in_bs, cudaStream_t st);
+// The same down the `ncols` columns of row-major arrays (row strides in_rs,
+// z_rs), and the split of the h complex rows it leads to into 2h real rows.
+void launch_real_pre_cols(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
+                          uint32_t ncols, uint64_t in_rs, uint64_t z_rs, cudaStream_t st);
+void launch_split_rows(const vec2_t* z, real_t* out, uint32_t h, uint32_t ncols, cudaStream_t st);
 // Odd-N helpers: real -> complex widening and complex -> real narrowing with scale.
 void launch_widen(const real_t* in, vec2_t* out, uint64_t n, cudaStream_t st);
 void launch_narrow(const vec2_t* in, real_t* out, uint64_t n, cudaStream_t st);
@@ -310,6 +315,9 @@ inline CopyRange copy_range(size_t b0, size_t b1, size_t total, bool first, bool
 // the padded lane plus the skew with the fewest bank conflicts.
 uint32_t spec_lane_stride(uint32_t R, uint32_t C, bool load_lane, bool store_lane,
                           uint32_t threads);
+// true when every pass of a direct plan run down the columns of a row-major
+// array gets tiles of four columns or more (32-byte row segments)
+bool columns_coalesce(const FftPlan& P);
 PassDesc make_pass_desc(const FftPlan& P, size_t pass, const vec2_t* in, const Layout& lin,
                         vec2_t* out, const Layout& lout, real_t scale);
 

@@ -60,6 +60,15 @@ static uint32_t tile_capacity() {
     return uint32_t(double(kSmemBudget - 64) / per);
 }
 
+bool columns_coalesce(const FftPlan& P) {
+    if (P.method != METHOD_DIRECT) return false;
+    // a column pass's tile takes min(16, capacity / R) columns: four or more
+    // keep its row segments at 32 bytes or longer
+    for (const PassSpec& s : P.passes)
+        if (uint64_t(s.R) * 4 > tile_capacity()) return false;
+    return true;
+}
+
 static uint32_t smem_for(uint32_t elems) {
     return 2u * (pad_host(elems) + 1u) * uint32_t(sizeof(vec2_t));
 }

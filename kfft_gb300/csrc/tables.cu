@@ -242,6 +242,78 @@ void launch_real_pre(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t
     count_launch();
 }
 
+// The same pre-processing down the columns of a row-major array: sequence c
+// is column c (element k at row k), of `ncols` columns; row strides in_rs and
+// z_rs.  Consecutive threads take consecutive columns.
+__global__ void k_real_pre_cols(const vec2_t* __restrict__ in, vec2_t* __restrict__ z,
+                                const vec2_t* __restrict__ stt, uint32_t h, uint32_t ncols,
+                                uint64_t in_rs, uint64_t z_rs) {
+    const uint32_t half = h / 2;
+    const uint64_t total = (uint64_t(half) + 1) * ncols;
+    for (uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; t < total;
+         t += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t k = uint32_t(t / ncols);
+        const uint32_t c = uint32_t(t - uint64_t(k) * ncols);
+        auto I = [&](uint32_t r) { return in[uint64_t(r) * in_rs + c]; };
+        vec2_t* Z = z + c;
+        if (k == 0) {
+            const vec2_t a = I(0), b = I(h);
+            Z[0] = {a.x + b.x, a.x - b.x};
+            continue;
+        }
+        vec2_t fk = I(k);
+        vec2_t fn = I(h - k);
+        vec2_t fnkc = {fn.x, -fn.y};
+        vec2_t fek = cadd_t(fk, fnkc), tmp = csub_t(fk, fnkc);
+        vec2_t fok = cmul_t(tmp, stt[k - 1]);
+        vec2_t lo = cadd_t(fek, fok);
+        vec2_t hi = csub_t(fek, fok);
+        hi.y = -hi.y;
+        if (2 * k == h) {
+            Z[uint64_t(k) * z_rs] = hi;
+        } else {
+            Z[uint64_t(k) * z_rs] = lo;
+            Z[uint64_t(h - k) * z_rs] = hi;
+        }
+    }
+}
+
+void launch_real_pre_cols(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
+                          uint32_t ncols, uint64_t in_rs, uint64_t z_rs, cudaStream_t st) {
+    uint64_t total = (uint64_t(h / 2) + 1) * ncols;
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (!blocks) return;
+    k_real_pre_cols<<<uint32_t(blocks), 256, 0, st>>>(in, z, st_tab, h, ncols, in_rs, z_rs);
+    note_cuda_error(cudaGetLastError());
+    count_launch();
+}
+
+// Column-wise complex results of h rows to 2h real rows: row 2m gets the real
+// parts of row m, row 2m+1 its imaginary parts (the even-length real inverse
+// run down the columns).
+__global__ void k_split_rows(const vec2_t* __restrict__ z, real_t* __restrict__ out, uint32_t h,
+                             uint32_t ncols) {
+    const uint64_t total = uint64_t(h) * ncols;
+    for (uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; t < total;
+         t += uint64_t(gridDim.x) * blockDim.x) {
+        const uint64_t m = t / ncols, c = t - m * ncols;
+        const vec2_t v = z[t];
+        out[(2 * m) * ncols + c] = v.x;
+        out[(2 * m + 1) * ncols + c] = v.y;
+    }
+}
+
+void launch_split_rows(const vec2_t* z, real_t* out, uint32_t h, uint32_t ncols, cudaStream_t st) {
+    uint64_t total = uint64_t(h) * ncols;
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (!blocks) return;
+    k_split_rows<<<uint32_t(blocks), 256, 0, st>>>(z, out, h, ncols);
+    note_cuda_error(cudaGetLastError());
+    count_launch();
+}
+
 __global__ void k_widen(const real_t* __restrict__ in, vec2_t* __restrict__ out, uint64_t n) {
     for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
          i += uint64_t(gridDim.x) * blockDim.x)

@@ -176,6 +176,23 @@ def test_2d_vs_oracle(lib, shape):
     assert rel_l2(lib.irfft2(S), O.irfft2(S)) <= t
 
 
+@pytest.mark.parametrize("shape", [(6, 10), (64, 48), (2, 7), (9, 8), (256, 100), (8192, 16),
+                                   (4096, 33)])
+def test_irfft2_any_spectrum_vs_oracle(lib, libf, shape):
+    """The real 2D inverse of a spectrum that is not Hermitian: the result
+    depends on which bins the transform reads, so it must read the same ones
+    as the reference (rows 0..y/2 of the row transforms for an even y, every
+    row for an odd y), normalised and not.  The shapes take both the
+    column path and the transposes (y = 8192 in FP32, y = 4096 in FP64)."""
+    rng = np.random.default_rng(sum(shape) + 5)
+    S = cx(rng, *shape)
+    t = tol64(shape[0] * shape[1])
+    for flags in (0, K.FLAG_DISABLE_NORM):
+        ref = O.irfft2(S, flags | O.FLAG_INVERSE) if flags else O.irfft2(S)
+        assert rel_l2(lib.irfft2(S, K.FLAG_INVERSE | flags), ref) <= t, flags
+        assert rel_l2(libf.irfft2(S.astype(np.complex64), K.FLAG_INVERSE | flags), ref) <= TOL32, flags
+
+
 def test_conv_fixtures(lib, golden):
     sizes = sorted(int(k.split("_")[-1]) for k in golden.files if k.startswith("cc_a_"))
     for n in sizes:
