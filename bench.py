@@ -929,7 +929,8 @@ def aggregate_over_ranks(ms_total, flops_per_step, steps, world, dist=None, devi
 # pass launches).  The uneven batch is too large for a full-set capture:
 # every 8th sequence was captured (37.47 M points, 2.708 GB) and scaled by
 # points, which the same length mix allows.
-NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.708141e9 / 37465227}
+NCU_DRAM_BYTES_PER_POINT = {"uneven_float": 2.708141e9 / 37465227,
+                            "uneven_double": 5.925791e9 / 37465227}
 NCU_DRAM_BYTES_PER_LAUNCH = {"c2c_f32_4096x4096": 217.3e6, "c2c_f32_2p18x64": 216.7e6,
                              "c2c_f32_2p20x16": 215.7e6, "c2c_f32_2p24": 215.9e6,
                              "c2c4096": 18.7e6}
