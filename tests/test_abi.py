@@ -83,6 +83,17 @@ def test_size_query_protocol(clib):
     assert clib.size_query("kfft_config2_cpx", 10, 11, 0) > s101
     assert clib.size_query("kfft_config_conv_cpx", 64, 0) > 0
     assert clib.size_query("kfft_config2_conv_scalar", 8, 8, 0) > 0
+    # a real conv2d plan of even x also holds the two plans of its
+    # half-spectrum inverse: its query exceeds the odd-x one by their sizes
+    even = clib.size_query("kfft_config2_conv_scalar", 8, 7, 0)
+    odd = clib.size_query("kfft_config2_conv_scalar", 9, 7, 0)
+    extra = (clib.size_query("kfft_config_cpx", 7, 1) +
+             clib.size_query("kfft_config_scalar", 8, 1))
+    base_even = (clib.size_query("kfft_config2_scalar", 8, 7, 0) +
+                 clib.size_query("kfft_config2_scalar", 8, 7, 1))
+    base_odd = (clib.size_query("kfft_config2_scalar", 9, 7, 0) +
+                clib.size_query("kfft_config2_scalar", 9, 7, 1))
+    assert even - base_even == odd - base_odd + extra
     # a user pool smaller than the query refuses and reports the size
     n = ctypes.c_size_t(s101 - 1)
     P = clib.L.kfft_pool_create(s101)
