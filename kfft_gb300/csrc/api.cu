@@ -275,15 +275,18 @@ bool run_cpx(const FftPlan& P, const vec2_t* din, vec2_t* dout, uint32_t batch, 
     return true;
 }
 
-// Column transform of a (rows=y, cols=x) complex array in place.
+// Column transform of a (rows=y, cols=x) complex array in place; `pitch`
+// (direct plans only; 0: x) is the row stride when only the first x columns
+// of wider rows are transformed.
 bool run_columns(const FftPlan& Py, vec2_t* data, uint32_t x, uint32_t y, real_t scale,
-                 Carve& cv, cudaStream_t st, const Product& pr = Product()) {
+                 Carve& cv, cudaStream_t st, const Product& pr = Product(), uint32_t pitch = 0) {
     if (pr.fused) *pr.fused = false;
+    if (pitch && pitch != x && Py.method != METHOD_DIRECT) return false;
     if (Py.method == METHOD_DIRECT) {
         Layout l;
         l.batch = x;
         l.bs = 1;
-        l.es = x;
+        l.es = pitch ? pitch : x;
         l.order = ORDER_B;
         size_t wb = workspace_bytes(Py, x);
         Workspace ws;
@@ -1264,11 +1267,29 @@ KFFT_API kfft_plan_s2d* kfft_config2_scalar(const uint32_t x_size, const uint32_
 }  // extern "C"
 
 namespace {
-// real 2D forward on device: rows real (expanded) -> complex columns
+// 1: an even-x real 2D forward transforms the columns of bins 0..x/2 only
+// and fills the rest by Hermitian symmetry
+#ifndef KFFT_S2D_FWD_HALF
+#define KFFT_S2D_FWD_HALF 1
+#endif
+// real 2D forward on device: rows real (expanded) -> complex columns.  For an
+// even x with a direct column plan, the rows keep bins 0..x/2, the columns run
+// over those x/2 + 1 only, and bins k2 > x/2 are filled from
+// X[k1][k2] = conj(X[-k1][x - k2]), the values the reference's columns of
+// conjugate-mirrored row bins come to.
 bool s2d_forward_dev(const kfft_plan_s2d* p, const real_t* din, vec2_t* dout, Carve& cv,
                      cudaStream_t st, const Product& pr = Product()) {
     const kfft_plan_sclr* rx = reinterpret_cast<const kfft_plan_sclr*>(p->plan_x);
     const kfft_plan_cpx* cy = reinterpret_cast<const kfft_plan_cpx*>(p->plan_y);
+    if (KFFT_S2D_FWD_HALF && !pr.mul && p->x % 2 == 0 && p->x >= 4 &&
+        gp(cy)->method == METHOD_DIRECT) {
+        const uint32_t hx = p->x / 2 + 1;
+        if (pr.fused) *pr.fused = false;
+        if (!real_forward_dev(rx, din, dout, p->y, p->x, 0, cv, st)) return false;
+        if (!run_columns(*gp(cy), dout, hx, p->y, real_t(1), cv, st, Product(), p->x)) return false;
+        launch_hermitian_fill(dout, p->x, p->y, st);
+        return true;
+    }
     if (!real_forward_dev(rx, din, dout, p->y, p->x, 1, cv, st)) return false;
     return run_columns(*gp(cy), dout, p->x, p->y, real_t(1), cv, st, pr);
 }

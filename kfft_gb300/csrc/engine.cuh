@@ -163,6 +163,9 @@ void launch_real_pre(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t
 void launch_real_pre_cols(const vec2_t* in, vec2_t* z, const vec2_t* st_tab, uint32_t h,
                           uint32_t ncols, uint64_t in_rs, uint64_t z_rs, cudaStream_t st);
 void launch_split_rows(const vec2_t* z, real_t* out, uint32_t h, uint32_t ncols, cudaStream_t st);
+// Bins x/2+1 .. x-1 of a y-by-x 2D spectrum of real data from bins 0..x/2
+// (x even, in place).
+void launch_hermitian_fill(vec2_t* data, uint32_t x, uint32_t y, cudaStream_t st);
 // Odd-N helpers: real -> complex widening and complex -> real narrowing with scale.
 void launch_widen(const real_t* in, vec2_t* out, uint64_t n, cudaStream_t st);
 void launch_narrow(const vec2_t* in, real_t* out, uint64_t n, cudaStream_t st);

@@ -314,6 +314,31 @@ void launch_split_rows(const vec2_t* z, real_t* out, uint32_t h, uint32_t ncols,
     count_launch();
 }
 
+// Bins x/2+1 .. x-1 of each row of a y-by-x 2D spectrum of real data from
+// the computed half: X[k1][k2] = conj(X[(y - k1) mod y][x - k2]) (x even).
+__global__ void k_hermitian_fill(vec2_t* __restrict__ data, uint32_t x, uint32_t y) {
+    const uint32_t w = x / 2 - 1;  // filled bins per row
+    const uint64_t total = uint64_t(w) * y;
+    for (uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; t < total;
+         t += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t k1 = uint32_t(t / w);
+        const uint32_t k2 = x / 2 + 1 + uint32_t(t - uint64_t(k1) * w);
+        const uint32_t r = k1 ? y - k1 : 0;
+        const vec2_t v = data[uint64_t(r) * x + (x - k2)];
+        data[uint64_t(k1) * x + k2] = {v.x, -v.y};
+    }
+}
+
+void launch_hermitian_fill(vec2_t* data, uint32_t x, uint32_t y, cudaStream_t st) {
+    const uint64_t total = uint64_t(x / 2 - 1) * y;
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (!blocks) return;
+    k_hermitian_fill<<<uint32_t(blocks), 256, 0, st>>>(data, x, y);
+    note_cuda_error(cudaGetLastError());
+    count_launch();
+}
+
 __global__ void k_widen(const real_t* __restrict__ in, vec2_t* __restrict__ out, uint64_t n) {
     for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
          i += uint64_t(gridDim.x) * blockDim.x)
